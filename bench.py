@@ -1,0 +1,384 @@
+"""Benchmark of the GPU source insertion (one JSON line on stdout).
+
+A step is one complete ``insert_source_in_cube`` equivalent on the GPU for
+the 1M-particle WendlandC2 disc on a 512 x 512 x 256 cube (thermal Gaussian
+lines): footprint binning, spectra, kernel weights, contraction, cube write
+and FP64 flux sums, from particle arrays resident in HBM.  The metric is
+cubes/s (higher is better); the line also carries particle-channel
+updates/s, the roofline of the dominant kernel (the contraction), the CPU
+baseline (the reference algorithm's per-pixel loop, restated in numpy and
+run on the host cores on a bounded pixel sample) and an end-to-end number
+through the C ABI with host buffers.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp32|bf16x3]
+    python bench.py --impl reference ...   # the CPU reference arm
+
+Under torchrun (N > 1) every rank inserts its own cube (independent
+replicas, weak scaling); rank 0 prints the line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "disc1m_512"
+METRIC = "cubes/s & particle-channel updates/s: FP32 vs BF16-split TC, <=1e-5 err vs FP64"
+L2_BYTES = 129 * 1024 * 1024
+# kernels of one mg_insert: tile init, edges, prep, 3 (pair scan), plan, emit,
+# 3 radix passes x (hist, 3 scan, scatter), segments, 2 x 3 (item scans),
+# partial check, contraction, split-K reduce, 2 flux
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 3 + 1 + 1 + 3 * 5 + 1 + 6 + 1 + 1 + 1 + 2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--form", default="f16x3", choices=["fp32", "bf16x3", "f16x3"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--n", type=int, default=None, help="override particle count")
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's per-pixel algorithm (oracle port), bounded
+# ---------------------------------------------------------------------------
+
+
+def cpu_baseline(w, budget_s, threads=None):
+    """Time the reference algorithm on the host cores on a sample and scale.
+
+    Spectra: ``init_spectra`` over a random particle subset (scaled by N /
+    subset).  Insertion: ``_evaluate_pixel_spectrum`` over random pixels of
+    the cube with a thread pool (scaled by N_pix / sample).  Returns
+    (cubes/s, threads, sample description).
+    """
+    from oracle import martini_oracle as orc
+    threads = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    n = w["n"]
+    kernels = ([orc.kernel_constants(orc.KT_WENDLAND_C2), orc.kernel_constants(orc.KT_DIRAC),
+                orc.kernel_constants(orc.KT_GAUSSIAN, 6.0)]
+               if w["kernel_name"] == "WendlandC2Kernel" else orc.adaptive_tuple(w["kernel_name"]))
+    sig = (w["sigma"].astype(np.float64) if w["sigma"] is not None
+           else np.full(n, w["sigma_const"]))
+    model = "dirac" if w["spectral_kind"] == "dirac" else "gaussian"
+    # spectra on a subset
+    sub = min(n, 50_000)
+    idx = rng.choice(n, sub, replace=False)
+    t0 = time.perf_counter()
+    orc.init_spectra(model, w["mHI"][idx], w["dist"][idx], w["v"][idx], w["edges"], sig[idx])
+    t_spec = (time.perf_counter() - t0) * n / sub
+    spectra = orc.init_spectra(model, w["mHI"], w["dist"], w["v"], w["edges"], sig)
+    kidx = (w["kernel_index"].astype(np.int64) if w["kernel_index"] is not None
+            else np.zeros(n, np.int64))
+    npix = w["nx"] * w["ny"]
+    args = (w["x"], w["y"], w["sm_range"], kernels, kidx, w["h_eff"].astype(np.float64), spectra)
+    # grow the pixel sample until the budget is used
+    done = 0
+    t_pix = 0.0
+    batch = 64
+    while t_pix < budget_s and done < npix:
+        pix = [(int(i), int(j)) for i, j in zip(rng.integers(0, w["nx"], batch),
+                                                rng.integers(0, w["ny"], batch))]
+        t0 = time.perf_counter()
+        orc.insert_perpixel(w["nx"], w["ny"], *args, ncpu=threads, pixels=pix)
+        t_pix += time.perf_counter() - t0
+        done += batch
+        batch = min(batch * 2, 4096)
+    t_cube = t_spec + t_pix * npix / done
+    desc = (f"reference per-pixel loop (numpy restatement) on {done} random pixels of "
+            f"{npix} and spectra of {sub} of {n} particles, scaled to one cube; "
+            f"{threads} threads")
+    return 1.0 / t_cube, threads, desc
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        for line in open(self.path):
+            p = [s.strip() for s in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                  "sw_power_cap"), p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        return reference_arm(a, rank, world)
+
+    import torch
+    import torch.distributed as dist
+    from martini_gb300 import _native as N
+    from martini_gb300 import workloads
+    from martini_gb300.engine import DeviceParticles, InsertionEngine
+
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    w = workloads.build(a.workload, n=a.n)
+    form = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}[a.form]
+    eng = InsertionEngine(dev)
+    parts = DeviceParticles.from_host(dev, w["x"], w["y"], w["sm_range"], w["h_eff"],
+                                      w["kernel_index"], v=w["v"], sigma=w["sigma"], amp=w["amp"])
+    edges = torch.from_numpy(np.ascontiguousarray(w["edges"])).to(dev)
+    nx, ny, nc = w["nx"], w["ny"], w["nc"]
+    cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=dev)
+    flux = torch.empty(nc + 1, dtype=torch.float64, device=dev)
+    prob = eng.problem(parts, w["kernels"], w["spectral_model"], w["sigma_const"], nx, ny, nc, 0,
+                       0, edges, cube, flux, form)
+    info = eng.plan(prob)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        eng.run(prob)
+
+    # the clock sampler starts before the warm-up: nvidia-smi's start-up
+    # stalls the GPU for a moment and must not fall into the timed region
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(1.5)
+    for _ in range(a.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    eng.check()
+
+    # --- timed region: K full insertions, L2 flushed between steps ----------
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(a.steps)]
+    for k in range(a.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    t_steps = sum(s.elapsed_time(e) for s, e in ev) / 1e3  # s
+    eng.check()
+
+    # --- dominant kernel: the contraction stage alone ------------------------
+    eng.run_stages(prob, N.MG_STAGE_BIN)
+    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(3)]
+    for s, e in cev:
+        flush.zero_()
+        s.record(stream)
+        eng.run_stages(prob, N.MG_STAGE_CONTRACT)
+        e.record(stream)
+    torch.cuda.synchronize()
+    t_contract = float(np.mean([s.elapsed_time(e) for s, e in cev])) / 1e3
+
+    # --- end to end through the C ABI with host buffers -------------------------
+    host = {k: torch.from_numpy(np.ascontiguousarray(w[k], dtype=dt)).pin_memory()
+            for k, dt in (("x", np.float64), ("y", np.float64), ("sm_range", np.float64),
+                          ("h_eff", np.float32), ("v", np.float64), ("amp", np.float64))}
+    if w["kernel_index"] is not None:
+        host["kernel_index"] = torch.from_numpy(w["kernel_index"].astype(np.int8)).pin_memory()
+    if w["sigma"] is not None:
+        host["sigma"] = torch.from_numpy(w["sigma"].astype(np.float32)).pin_memory()
+    host_cube = torch.empty((nx, ny, nc), dtype=torch.float32).pin_memory()
+    host_flux = torch.empty(nc + 1, dtype=torch.float64).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = host_cube.numel() * 4 + host_flux.numel() * 8
+    dev_parts = {k: getattr(parts, k) for k in host}
+
+    def e2e_step():
+        for k, t in host.items():
+            dev_parts[k].copy_(t, non_blocking=True)
+        eng.run(prob)
+        host_cube.copy_(cube, non_blocking=True)
+        host_flux.copy_(flux, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    ke = max(1, min(a.steps, 5))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(ke):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = e0.elapsed_time(e1) / 1e3 / ke
+
+    # --- aggregate over ranks ---------------------------------------------------
+    if world > 1:
+        tt = torch.tensor([t_steps, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_steps, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # algorithmic work: box-footprint pixels x channels (the reference's
+    # per-pixel mask selects exactly these pairs)
+    F = workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], nx, ny)
+    updates = float(F.sum()) * nc
+    flops = 2.0 * updates
+    cubes_per_s = world * a.steps / t_steps
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak_tf = peaks.get("bf16_tflops", 1900.0)
+    achieved_tf = flops / t_contract / 1e12
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", f"traffic_{a.workload}_{a.form}.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("bytes_per_launch")
+    line = {
+        "metric": METRIC,
+        "value": cubes_per_s,
+        "unit": "cubes/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": t_steps / a.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": a.form,
+        "data": "synthetic (seeded exponential disc, no dataset)",
+        "config": {"workload": a.workload, "particles": w["n"], "particles_generated":
+                   w["n_input"], "cube": [nx, ny, nc], "kernel": w["kernel_name"],
+                   "spectrum": w["spectral_kind"], "form": a.form,
+                   "l2": "flushed between steps (256 MiB write)", "parallelism":
+                   f"replicas{world}", "pairs": int(info.n_pairs), "items": int(info.n_items)},
+        "particle_channel_updates_per_s": world * updates * a.steps / t_steps,
+        "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf,
+                     "unit": "TFLOP/s", "frac": achieved_tf / peak_tf, "traffic": traffic,
+                     "kernel": "k_contract (+ split-K reduce)",
+                     "contract_ms": t_contract * 1e3,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks
+                     else "fallback 1.9 PFLOP/s"},
+        "e2e": {"value": world / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": LAUNCHES_PER_STEP * a.steps,
+        "step_ms": [round(s.elapsed_time(e), 3) for s, e in ev],
+        "clocks": clk,
+    }
+    if not a.no_cpu_baseline:
+        v, cores, desc = cpu_baseline(w, a.cpu_sample_s)
+        line["cpu_baseline"] = {"value": v, "unit": "cubes/s", "cores": cores, "kind": "port",
+                                "sample": desc}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def reference_arm(a, rank, world):
+    """The reference algorithm (per-pixel numpy restatement) on the host cores."""
+    if rank != 0:
+        return
+    from martini_gb300 import workloads
+    w = workloads.build(a.workload, n=a.n)
+    budget = max(2.0, 60.0 / max(1, a.steps + a.warmup))
+    for _ in range(a.warmup):
+        cpu_baseline(w, budget / 4)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        v, cores, desc = cpu_baseline(w, budget)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference",
+        "metric": METRIC, "value": value, "unit": "cubes/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded exponential disc, no dataset)",
+        "config": {"workload": a.workload, "particles": w["n"], "cube": [w["nx"], w["ny"], w["nc"]],
+                   "kernel": w["kernel_name"], "spectrum": w["spectral_kind"]},
+        "cpu_baseline": {"value": value, "unit": "cubes/s", "cores": cores, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": "cubes/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

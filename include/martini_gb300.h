@@ -1,0 +1,188 @@
+/*
+ * martini_gb300 -- C ABI of the GB300 source-insertion library.
+ *
+ * The library inserts SPH particles into a spectral data cube, i.e. it
+ * computes for every pixel (i, j) and channel c
+ *
+ *     cube[i][j][c] = sum_p  W_p(i, j) * S_p(c)                  [Jy / pix^2]
+ *
+ * where W_p is the SPH kernel integrated over pixel (i, j) and S_p the
+ * particle's channel spectrum.  This is MARTINI's
+ * ``Martini.insert_source_in_cube`` (reference: martini/martini.py:285-407)
+ * with the per-pixel contraction of ``_BaseMartini._evaluate_pixel_spectrum``
+ * (martini/martini.py:243-283), the kernel pixel integrals
+ * ``_BaseSPHKernel._px_weight`` / ``_kernel_integral``
+ * (martini/sph_kernels.py:85-119, :400-441, :544-685, :791-858, :994-1044,
+ * :1136-1165, :1330-1363, :1486-1564) and the spectra of
+ * ``_BaseSpectrum.init_spectra`` (martini/spectral_models.py:63-200,
+ * :386-425, :544-570).  The reference is pure Python and has no FFI; these
+ * entry points are what a ctypes/cffi binding of ``_insert_source_in_cube``
+ * calls.
+ *
+ * Conventions
+ *   - All array pointers are DEVICE pointers owned by the caller.
+ *   - Every call is asynchronous on the given stream unless stated.
+ *   - Return value: MG_OK or a negative MG_ERR_* code; a message for the
+ *     last error of the calling thread is available from mg_last_error().
+ *   - The cube layout is [i][j][c] (x = RA index slowest, channel fastest),
+ *     float32, the padded grid of the reference's DataCube._array.
+ */
+#ifndef MARTINI_GB300_H
+#define MARTINI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MG_OK 0
+#define MG_ERR_INVALID_ARGUMENT (-1)
+#define MG_ERR_CUDA (-2)
+#define MG_ERR_WORKSPACE (-3)      /* workspace too small for this problem */
+#define MG_ERR_NOT_MONOTONIC (-4)  /* channel edges not strictly monotonic */
+#define MG_ERR_UNSUPPORTED (-5)
+#define MG_ERR_TIMEOUT (-6)        /* a bounded device-side wait expired */
+
+/* SPH kernel types (martini/sph_kernels.py) */
+#define MG_KERNEL_WENDLAND_C2 0   /* _WendlandC2Kernel      :340-478   */
+#define MG_KERNEL_WENDLAND_C6 1   /* _WendlandC6Kernel      :481-721   */
+#define MG_KERNEL_CUBIC_SPLINE 2  /* _CubicSplineKernel     :724-894   */
+#define MG_KERNEL_QUARTIC_SPLINE 3 /* _QuarticSplineKernel  :1402-1600 */
+#define MG_KERNEL_GAUSSIAN 4      /* _GaussianKernel(trunc) :897-1080  */
+#define MG_KERNEL_DIRAC 5         /* DiracDeltaKernel       :1083-1204 */
+
+/* spectral models (martini/spectral_models.py) */
+#define MG_SPECTRUM_GAUSSIAN 0    /* GaussianSpectrum  :304-485 */
+#define MG_SPECTRUM_DIRAC 1       /* DiracDeltaSpectrum :488-587 */
+#define MG_SPECTRUM_TABLE 2       /* caller-supplied spectra[n][nc] (any model) */
+
+/* contraction forms */
+#define MG_FORM_FP32 0            /* FP32 CUDA-core contraction */
+#define MG_FORM_BF16X3 1          /* BF16 hi+lo split, three tcgen05 products */
+#define MG_FORM_F16X3 2           /* FP16 hi+lo split (power-of-two scaled), three tcgen05 products */
+
+#define MG_MAX_KERNELS 4
+
+typedef struct mg_kernel_spec {
+  int32_t type;      /* MG_KERNEL_* */
+  float truncate;    /* Gaussian truncation in sigma (MG_KERNEL_GAUSSIAN only) */
+} mg_kernel_spec;
+
+/*
+ * One insertion problem: particles already projected to pixel coordinates
+ * (the state the reference holds after Martini.__init__: source.pixcoords,
+ * sph_kernel.sm_lengths/_rescale/sm_ranges/kernel_indices, spectral inputs).
+ */
+typedef struct mg_problem {
+  int64_t n;                   /* particle count (may be 0) */
+  const double* x;             /* [n] pixel coordinate on axis 0 (0-based, padded) */
+  const double* y;             /* [n] pixel coordinate on axis 1 */
+  const double* sm_range;      /* [n] footprint half-width, px (sph_kernel.sm_ranges) */
+  const float* h_eff;          /* [n] sm_lengths * _rescale, px */
+  const int8_t* kernel_index;  /* [n] index into kernels[], -1 means kernels[0]; NULL = all 0 */
+  int32_t n_kernels;           /* 1..MG_MAX_KERNELS */
+  mg_kernel_spec kernels[MG_MAX_KERNELS];
+
+  int32_t spectral_model;      /* MG_SPECTRUM_* */
+  const double* v;             /* [n] line-of-sight velocity, km/s (GAUSSIAN/DIRAC) */
+  const float* sigma;          /* [n] Gaussian width, km/s, or NULL to use sigma_const */
+  float sigma_const;
+  const double* amp;           /* [n] mHI / D^2 / 2.36e5 (Jy km/s) (GAUSSIAN/DIRAC) */
+  const float* spectra;        /* [n][nc] Jy (TABLE only) */
+
+  int32_t nx, ny, nc;          /* padded cube size */
+  int32_t padx, pady;          /* pad on each side (flux sums skip it) */
+  const double* edges;         /* [nc+1] channel edges, km/s, strictly monotonic */
+  float* cube;                 /* [nx][ny][nc] output, Jy / pix^2, overwritten */
+  double* flux;                /* optional [nc+1]: total flux (Jy), then per channel; NULL = skip */
+  int32_t form;                /* MG_FORM_* */
+} mg_problem;
+
+/* sizes reported by mg_plan */
+typedef struct mg_plan_info {
+  int64_t n_pairs;          /* (tile, particle) pairs after footprint binning */
+  int64_t n_items;          /* reserved (0) */
+  int64_t n_partial_items;  /* upper bound on split-K partial tiles */
+  int64_t n_tiles;
+  size_t workspace_bytes;   /* mg_workspace_size(p, n_pairs, n_partial_items) */
+} mg_plan_info;
+
+/* Library version string. */
+const char* mg_version(void);
+
+/* Message for the last error returned on the calling thread. */
+const char* mg_last_error(void);
+
+/*
+ * Workspace bytes needed for a problem of this shape with room for
+ * max_pairs (tile, particle) pairs and max_partial_items split-K partial
+ * tiles (the counts mg_plan reports).
+ */
+int mg_workspace_size(const mg_problem* p, int64_t max_pairs, int64_t max_partial_items,
+                      size_t* bytes);
+
+/*
+ * Bin the particles and report the exact pair/item counts and the workspace
+ * size mg_insert needs.  Needs a workspace of at least
+ * mg_workspace_size(p, 0, 0).  SYNCHRONISES the stream (it reads the counts
+ * back).  Returns MG_ERR_NOT_MONOTONIC if the channel edges are not strictly
+ * monotonic.
+ */
+int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* stream,
+            mg_plan_info* info);
+
+/*
+ * Full insertion: footprint binning, spectra, kernel weights, contraction,
+ * cube write and (if p->flux) the FP64 flux sums.  Asynchronous on stream;
+ * no host synchronisation and no allocation, so it can be captured in a
+ * CUDA graph.  The workspace must have been sized by mg_workspace_size with
+ * the same max_pairs / max_partial_items.  If the data need more than that,
+ * the device code skips the contraction and mg_check() returns
+ * MG_ERR_WORKSPACE.
+ */
+int mg_insert(const mg_problem* p, void* workspace, size_t workspace_bytes, int64_t max_pairs,
+              int64_t max_partial_items, void* stream);
+
+/* stages of mg_insert_stages (bit mask) */
+#define MG_STAGE_BIN 1        /* records, tile histogram, plan, tile-major list */
+#define MG_STAGE_CONTRACT 2   /* cube clear, contraction, split-K reduction */
+#define MG_STAGE_FLUX 4       /* FP64 flux sums (if p->flux) */
+#define MG_STAGE_ALL 7
+
+/*
+ * mg_insert restricted to some stages, in order, on the same workspace
+ * (a stage reads what the previous ones left there).  For timing stages
+ * separately; mg_insert == mg_insert_stages(..., MG_STAGE_ALL, ...).
+ */
+int mg_insert_stages(const mg_problem* p, void* workspace, size_t workspace_bytes,
+                     int64_t max_pairs, int64_t max_partial_items, int32_t stages, void* stream);
+
+/*
+ * Read back the device status word of the last mg_plan/mg_insert on this
+ * workspace (SYNCHRONISES the stream).  Returns MG_OK, MG_ERR_WORKSPACE,
+ * MG_ERR_NOT_MONOTONIC or MG_ERR_TIMEOUT.
+ */
+int mg_check(void* workspace, void* stream);
+
+/*
+ * Materialise the spectra of a GAUSSIAN/DIRAC problem: out[n][nc] in Jy,
+ * the reference's spectral_model.spectra (spectral_models.py:63-147).
+ */
+int mg_spectra(const mg_problem* p, float* out, void* stream);
+
+/*
+ * FP64 flux sums of a cube already in device memory: flux[0] = total over
+ * the unpadded region, flux[1 + c] = per channel (martini/martini.py:367-392).
+ */
+int mg_flux(const float* cube, int32_t nx, int32_t ny, int32_t nc, int32_t padx,
+            int32_t pady, double* flux, void* workspace, size_t workspace_bytes,
+            void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MARTINI_GB300_H */

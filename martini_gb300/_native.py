@@ -1,0 +1,125 @@
+"""ctypes binding of the in-tree CUDA library ``libmartini_gb300.so``.
+
+The library is the product: there is no CPU fallback.  Loading fails loudly
+if the library has not been built (``python -m martini_gb300.build`` or
+``__graft_entry__.build()``) or no CUDA device is present.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmartini_gb300.so")
+
+MG_OK = 0
+MG_ERR_INVALID_ARGUMENT = -1
+MG_ERR_CUDA = -2
+MG_ERR_WORKSPACE = -3
+MG_ERR_NOT_MONOTONIC = -4
+MG_ERR_UNSUPPORTED = -5
+MG_ERR_TIMEOUT = -6
+
+MG_KERNEL_WENDLAND_C2 = 0
+MG_KERNEL_WENDLAND_C6 = 1
+MG_KERNEL_CUBIC_SPLINE = 2
+MG_KERNEL_QUARTIC_SPLINE = 3
+MG_KERNEL_GAUSSIAN = 4
+MG_KERNEL_DIRAC = 5
+
+MG_SPECTRUM_GAUSSIAN = 0
+MG_SPECTRUM_DIRAC = 1
+MG_SPECTRUM_TABLE = 2
+
+MG_FORM_FP32 = 0
+MG_FORM_BF16X3 = 1
+MG_FORM_F16X3 = 2
+
+MG_MAX_KERNELS = 4
+
+# every symbol include/martini_gb300.h declares
+EXPORTS = ("mg_version", "mg_last_error", "mg_workspace_size", "mg_plan", "mg_insert",
+           "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux")
+
+MG_STAGE_BIN = 1
+MG_STAGE_CONTRACT = 2
+MG_STAGE_FLUX = 4
+MG_STAGE_ALL = 7
+
+
+class KernelSpec(C.Structure):
+    _fields_ = [("type", C.c_int32), ("truncate", C.c_float)]
+
+
+class Problem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("x", C.c_void_p), ("y", C.c_void_p), ("sm_range", C.c_void_p), ("h_eff", C.c_void_p),
+        ("kernel_index", C.c_void_p),
+        ("n_kernels", C.c_int32),
+        ("kernels", KernelSpec * MG_MAX_KERNELS),
+        ("spectral_model", C.c_int32),
+        ("v", C.c_void_p), ("sigma", C.c_void_p), ("sigma_const", C.c_float),
+        ("amp", C.c_void_p), ("spectra", C.c_void_p),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nc", C.c_int32),
+        ("padx", C.c_int32), ("pady", C.c_int32),
+        ("edges", C.c_void_p), ("cube", C.c_void_p), ("flux", C.c_void_p),
+        ("form", C.c_int32),
+    ]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("n_pairs", C.c_int64), ("n_items", C.c_int64), ("n_partial_items", C.c_int64),
+                ("n_tiles", C.c_int64), ("workspace_bytes", C.c_size_t)]
+
+
+class MartiniGB300Error(RuntimeError):
+    """A non-zero status from the native library."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"martini_gb300 error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load (once) and return the native library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build it with `python -m martini_gb300.build` "
+            "(the GPU path has no CPU fallback)")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    lib.mg_version.restype = C.c_char_p
+    lib.mg_last_error.restype = C.c_char_p
+    lib.mg_workspace_size.argtypes = [P(Problem), C.c_int64, C.c_int64, P(C.c_size_t)]
+    lib.mg_plan.argtypes = [P(Problem), C.c_void_p, C.c_size_t, C.c_void_p, P(PlanInfo)]
+    lib.mg_insert.argtypes = [P(Problem), C.c_void_p, C.c_size_t, C.c_int64, C.c_int64,
+                              C.c_void_p]
+    lib.mg_insert_stages.argtypes = [P(Problem), C.c_void_p, C.c_size_t, C.c_int64, C.c_int64,
+                                     C.c_int32, C.c_void_p]
+    lib.mg_check.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mg_spectra.argtypes = [P(Problem), C.c_void_p, C.c_void_p]
+    lib.mg_flux.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                            C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    for f in ("mg_workspace_size", "mg_plan", "mg_insert", "mg_insert_stages", "mg_check",
+              "mg_spectra", "mg_flux"):
+        getattr(lib, f).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    """Raise MartiniGB300Error (ValueError for non-monotonic edges) on failure."""
+    if rc == MG_OK:
+        return
+    msg = load().mg_last_error().decode(errors="replace")
+    if rc == MG_ERR_NOT_MONOTONIC:
+        raise ValueError(msg)
+    raise MartiniGB300Error(rc, msg)

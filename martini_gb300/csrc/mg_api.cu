@@ -1,0 +1,433 @@
+// C ABI of the martini_gb300 library (declared in include/martini_gb300.h).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "mg_internal.cuh"
+
+using namespace mg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(MG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Segment shape of a contraction form: channel blocks per tile and their width.
+void seg_shape(int form, int nc, int* ncb, int* width) {
+  if (form == MG_FORM_BF16X3 || form == MG_FORM_F16X3) {
+    *ncb = 1;
+    *width = (nc + 15) / 16 * 16;
+  } else {
+    *ncb = (nc + CBLK - 1) / CBLK;
+    *width = CBLK;
+  }
+}
+
+int channel_bits(int nc) {
+  int b = 0;
+  while ((1 << b) < nc) ++b;
+  return b;
+}
+
+struct Layout {
+  size_t hdr, rec, npairs, pair_off, tile_count, tile_wlo, tile_whi, tile_off, ehi, elo, inv_w,
+      keys, list, keys_tmp, list_tmp, rs_hist, rs_off, scan_sums, seg_lo, seg_hi, seg_items,
+      seg_part, item_off, part_off, partial, flux_part, total;
+  int nseg, ncb, width;
+};
+
+Layout layout(long long n, int ntiles, int nc, int form, int flux_ch, long long cap_pairs,
+              long long cap_partial) {
+  Layout L;
+  seg_shape(form, nc, &L.ncb, &L.width);
+  L.nseg = ntiles * L.ncb;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o += align256(bytes > 0 ? bytes : 1);
+    return at;
+  };
+  const size_t nn = (size_t)(n > 0 ? n : 1);
+  const size_t cp = (size_t)(cap_pairs > 0 ? cap_pairs : 1);
+  const long long rb = radix_blocks(cap_pairs > 0 ? cap_pairs : 1);
+  long long scan_n = n;
+  if (256 * rb > scan_n) scan_n = 256 * rb;
+  if (L.nseg > scan_n) scan_n = L.nseg;
+  L.hdr = take(sizeof(WsHeader));
+  L.rec = take(sizeof(PRec) * nn);
+  L.npairs = take(sizeof(int) * nn);
+  L.pair_off = take(sizeof(long long) * nn);
+  L.tile_count = take(sizeof(int) * ntiles);
+  L.tile_wlo = take(sizeof(int) * ntiles);
+  L.tile_whi = take(sizeof(int) * ntiles);
+  L.tile_off = take(sizeof(long long) * (ntiles + 1));
+  L.ehi = take(sizeof(float) * (nc + 1));
+  L.elo = take(sizeof(float) * (nc + 1));
+  L.inv_w = take(sizeof(float) * nc);
+  L.keys = take(sizeof(unsigned) * cp);
+  L.list = take(sizeof(int) * cp);
+  L.keys_tmp = take(sizeof(unsigned) * cp);
+  L.list_tmp = take(sizeof(int) * cp);
+  L.rs_hist = take(sizeof(int) * 256 * (size_t)rb);
+  L.rs_off = take(sizeof(long long) * 256 * (size_t)rb);
+  L.scan_sums = take(sizeof(long long) * (size_t)(scan_blocks(scan_n) + 1));
+  L.seg_lo = take(sizeof(long long) * L.nseg);
+  L.seg_hi = take(sizeof(long long) * L.nseg);
+  L.seg_items = take(sizeof(int) * L.nseg);
+  L.seg_part = take(sizeof(int) * L.nseg);
+  L.item_off = take(sizeof(long long) * L.nseg);
+  L.part_off = take(sizeof(long long) * L.nseg);
+  L.flux_part = take(sizeof(double) * (size_t)flux_ch * nc);
+  L.partial = take(sizeof(float) * (size_t)TILE_PX * L.width * (size_t)(cap_partial > 0 ? cap_partial : 0));
+  L.total = o;
+  return L;
+}
+
+Ws make_ws(void* base, const Layout& L, int nc) {
+  char* b = static_cast<char*>(base);
+  Ws w;
+  w.hdr = reinterpret_cast<WsHeader*>(b + L.hdr);
+  w.rec = reinterpret_cast<PRec*>(b + L.rec);
+  w.npairs = reinterpret_cast<int*>(b + L.npairs);
+  w.pair_off = reinterpret_cast<long long*>(b + L.pair_off);
+  w.tile_count = reinterpret_cast<int*>(b + L.tile_count);
+  w.tile_wlo = reinterpret_cast<int*>(b + L.tile_wlo);
+  w.tile_whi = reinterpret_cast<int*>(b + L.tile_whi);
+  w.tile_off = reinterpret_cast<long long*>(b + L.tile_off);
+  w.ehi = reinterpret_cast<float*>(b + L.ehi);
+  w.elo = reinterpret_cast<float*>(b + L.elo);
+  w.inv_w = reinterpret_cast<float*>(b + L.inv_w);
+  w.keys = reinterpret_cast<unsigned*>(b + L.keys);
+  w.list = reinterpret_cast<int*>(b + L.list);
+  w.keys_tmp = reinterpret_cast<unsigned*>(b + L.keys_tmp);
+  w.list_tmp = reinterpret_cast<int*>(b + L.list_tmp);
+  w.rs_hist = reinterpret_cast<int*>(b + L.rs_hist);
+  w.rs_off = reinterpret_cast<long long*>(b + L.rs_off);
+  w.scan_sums = reinterpret_cast<long long*>(b + L.scan_sums);
+  w.seg_lo = reinterpret_cast<long long*>(b + L.seg_lo);
+  w.seg_hi = reinterpret_cast<long long*>(b + L.seg_hi);
+  w.seg_items = reinterpret_cast<int*>(b + L.seg_items);
+  w.seg_part = reinterpret_cast<int*>(b + L.seg_part);
+  w.item_off = reinterpret_cast<long long*>(b + L.item_off);
+  w.part_off = reinterpret_cast<long long*>(b + L.part_off);
+  w.partial = reinterpret_cast<float*>(b + L.partial);
+  w.flux_part = reinterpret_cast<double*>(b + L.flux_part);
+  w.nseg = L.nseg;
+  w.ncb_seg = L.ncb;
+  w.seg_width = L.width;
+  w.cbits = channel_bits(nc);
+  return w;
+}
+
+double gaussian_norm(double t) {
+  return std::erf(t / std::sqrt(2.0)) -
+         2.0 * t / std::sqrt(2.0 * 3.14159265358979323846) * std::exp(-t * t / 2.0);
+}
+
+// Validate the problem and fill device-side geometry (no device access:
+// edge direction and monotonicity are resolved by the k_edges kernel).
+int make_geo(const mg_problem* p, Geo* g) {
+  if (!p) return fail(MG_ERR_INVALID_ARGUMENT, "null problem");
+  if (p->nx <= 0 || p->ny <= 0 || p->nc <= 0)
+    return fail(MG_ERR_INVALID_ARGUMENT, "cube dimensions must be positive");
+  if (p->n < 0) return fail(MG_ERR_INVALID_ARGUMENT, "negative particle count");
+  if (p->n_kernels < 1 || p->n_kernels > MG_MAX_KERNELS)
+    return fail(MG_ERR_INVALID_ARGUMENT, "n_kernels must be 1..4");
+  if (p->padx < 0 || p->pady < 0 || 2 * p->padx >= p->nx || 2 * p->pady >= p->ny)
+    return fail(MG_ERR_INVALID_ARGUMENT, "invalid pad");
+  if (!p->edges || !p->cube) return fail(MG_ERR_INVALID_ARGUMENT, "edges and cube are required");
+  if (p->spectral_model == MG_SPECTRUM_TABLE) {
+    if (p->n > 0 && !p->spectra)
+      return fail(MG_ERR_INVALID_ARGUMENT, "TABLE spectral model needs spectra");
+  } else if (p->spectral_model == MG_SPECTRUM_GAUSSIAN || p->spectral_model == MG_SPECTRUM_DIRAC) {
+    if (p->n > 0 && (!p->v || !p->amp))
+      return fail(MG_ERR_INVALID_ARGUMENT, "v and amp are required");
+    if (p->n > 0 && p->spectral_model == MG_SPECTRUM_GAUSSIAN && !p->sigma &&
+        !(p->sigma_const > 0.f))
+      return fail(MG_ERR_INVALID_ARGUMENT, "Gaussian spectrum needs sigma > 0");
+  } else {
+    return fail(MG_ERR_INVALID_ARGUMENT, "unknown spectral model");
+  }
+  if (p->n > 0 && (!p->x || !p->y || !p->sm_range || !p->h_eff))
+    return fail(MG_ERR_INVALID_ARGUMENT, "x, y, sm_range and h_eff are required");
+  if (p->form != MG_FORM_FP32 && p->form != MG_FORM_BF16X3 && p->form != MG_FORM_F16X3)
+    return fail(MG_ERR_INVALID_ARGUMENT, "unknown contraction form");
+  std::memset(g, 0, sizeof(Geo));
+  g->nx = p->nx;
+  g->ny = p->ny;
+  g->nc = p->nc;
+  g->padx = p->padx;
+  g->pady = p->pady;
+  g->ntx = (p->nx + TILE_I - 1) / TILE_I;
+  g->nty = (p->ny + TILE_J - 1) / TILE_J;
+  long long nt = (long long)g->ntx * g->nty;
+  if (nt > (1LL << 30)) return fail(MG_ERR_INVALID_ARGUMENT, "cube too large");
+  g->ntiles = (int)nt;
+  g->n_kernels = p->n_kernels;
+  g->spectral_model = p->spectral_model;
+  g->sigma_const = p->sigma_const;
+  g->form = p->form;
+  for (int k = 0; k < p->n_kernels; ++k) {
+    int t = p->kernels[k].type;
+    if (t < MG_KERNEL_WENDLAND_C2 || t > MG_KERNEL_DIRAC)
+      return fail(MG_ERR_INVALID_ARGUMENT, "unknown kernel type");
+    g->ks[k].type = t;
+    g->ks[k].truncate = p->kernels[k].truncate;
+    if (t == MG_KERNEL_GAUSSIAN) {
+      if (!(p->kernels[k].truncate >= 2.f))
+        return fail(MG_ERR_INVALID_ARGUMENT,
+                    "GaussianKernel with truncation <2sigma will cause large errors in total mass.");
+      g->ks[k].gnorm = (float)gaussian_norm(p->kernels[k].truncate);
+    } else {
+      g->ks[k].gnorm = 1.f;
+    }
+  }
+  return MG_OK;
+}
+
+int num_sms() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+PrepArgs prep_args(const mg_problem* p) {
+  PrepArgs a;
+  a.n = p->n;
+  a.x = p->x;
+  a.y = p->y;
+  a.r = p->sm_range;
+  a.h = p->h_eff;
+  a.kidx = p->kernel_index;
+  a.v = p->v;
+  a.sigma = p->sigma;
+  a.amp = p->amp;
+  a.edges = p->edges;
+  a.spectra = p->spectra;
+  return a;
+}
+
+int workspace_view(const mg_problem* p, const Geo& g, void* ws, size_t bytes,
+                   long long cap_pairs, long long cap_partial, Ws* w) {
+  Layout L = layout(p->n, g.ntiles, g.nc, p->form, flux_chunks(g.nx, g.padx), cap_pairs,
+                    cap_partial);
+  if (!ws || bytes < L.total)
+    return fail(MG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(L.total) +
+                                      " bytes, have " + std::to_string(bytes));
+  *w = make_ws(ws, L, g.nc);
+  if (sort_bits(g, *w) > 32) return fail(MG_ERR_INVALID_ARGUMENT, "cube too large for the sort key");
+  return MG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mg_version(void) { return "martini_gb300 0.1 (sm_103a)"; }
+
+const char* mg_last_error(void) { return g_err.c_str(); }
+
+int mg_workspace_size(const mg_problem* p, int64_t max_pairs, int64_t max_partial_items,
+                      size_t* bytes) {
+  if (!p || !bytes) return fail(MG_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->nx <= 0 || p->ny <= 0 || p->nc <= 0 || p->n < 0)
+    return fail(MG_ERR_INVALID_ARGUMENT, "invalid problem dimensions");
+  if (max_pairs < 0 || max_partial_items < 0)
+    return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
+  int ntiles = ((p->nx + TILE_I - 1) / TILE_I) * ((p->ny + TILE_J - 1) / TILE_J);
+  *bytes = layout(p->n, ntiles, p->nc, p->form, flux_chunks(p->nx, p->padx), max_pairs,
+                  max_partial_items).total;
+  return MG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The stages of an insertion (MG_STAGE_* bits; `scatter` adds the particle
+// list to the binning stage); all asynchronous on stream s.
+int run(const mg_problem* p, void* ws, size_t bytes, cudaStream_t s, long long cap_pairs,
+        long long cap_partial, int stages, bool scatter, Ws* wout, Geo* gout) {
+  Geo g;
+  int rc = make_geo(p, &g);
+  if (rc) return rc;
+  if (cap_pairs < 0 || cap_partial < 0) return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
+  Ws w;
+  rc = workspace_view(p, g, ws, bytes, cap_pairs, cap_partial, &w);
+  if (rc) return rc;
+  if (stages & MG_STAGE_BIN) {
+    launch_prep(prep_args(p), g, w, num_sms(), s, cap_pairs, cap_partial);
+    if (scatter) launch_sort_segments(prep_args(p), g, w, cap_pairs, num_sms(), s);
+  }
+  cudaError_t e;
+  if (stages & MG_STAGE_CONTRACT) {
+    e = cudaMemsetAsync(p->cube, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nc, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&w.hdr->item_counter, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cube clear");
+    if (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) {
+      rc = launch_contract_bf16x3(g, w, p->spectra, p->cube, num_sms(), s);
+      if (rc == MG_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tensor-core kernel set-up");
+      if (rc) return fail(rc, "tensor-core form does not support this cube (band too wide)");
+    } else {
+      launch_contract_fp32(g, w, p->spectra, p->cube, num_sms(), s);
+    }
+  }
+  if ((stages & MG_STAGE_FLUX) && p->flux)
+    launch_flux(p->cube, p->nx, p->ny, p->nc, p->padx, p->pady, w.flux_part, p->flux, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  *wout = w;
+  *gout = g;
+  return MG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* stream,
+            mg_plan_info* info) {
+  if (!info) return fail(MG_ERR_INVALID_ARGUMENT, "null info");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Ws w;
+  Geo g;
+  int rc = run(p, workspace, workspace_bytes, s, 0, 0, MG_STAGE_BIN, false, &w, &g);
+  if (rc) return rc;
+  WsHeader h;
+  cudaError_t e = cudaMemcpyAsync(&h, w.hdr, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "mg_plan readback");
+  if (h.status & ST_EDGES) return fail(MG_ERR_NOT_MONOTONIC, "Channel edges are not monotonic sequence.");
+  info->n_pairs = h.n_pairs;
+  info->n_items = 0;
+  info->n_partial_items = h.partial_bound;
+  info->n_tiles = g.ntiles;
+  info->workspace_bytes = layout(p->n, g.ntiles, g.nc, p->form, flux_chunks(g.nx, g.padx),
+                                 h.n_pairs, h.partial_bound).total;
+  return MG_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int mg_insert(const mg_problem* p, void* workspace, size_t workspace_bytes, int64_t max_pairs,
+              int64_t max_partial_items, void* stream) {
+  return mg_insert_stages(p, workspace, workspace_bytes, max_pairs, max_partial_items,
+                          MG_STAGE_ALL, stream);
+}
+
+int mg_insert_stages(const mg_problem* p, void* workspace, size_t workspace_bytes,
+                     int64_t max_pairs, int64_t max_partial_items, int32_t stages, void* stream) {
+  if (stages & ~MG_STAGE_ALL) return fail(MG_ERR_INVALID_ARGUMENT, "unknown stage bits");
+  Ws w;
+  Geo g;
+  return run(p, workspace, workspace_bytes, static_cast<cudaStream_t>(stream), max_pairs,
+             max_partial_items, stages, true, &w, &g);
+}
+
+int mg_check(void* workspace, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!workspace) return fail(MG_ERR_INVALID_ARGUMENT, "null workspace");
+  WsHeader h;
+  cudaError_t e = cudaMemcpyAsync(&h, workspace, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "mg_check");
+  if (h.status & ST_EDGES)
+    return fail(MG_ERR_NOT_MONOTONIC, "Channel edges are not monotonic sequence.");
+  if (h.status & ST_TIMEOUT)
+    return fail(MG_ERR_TIMEOUT, "a device-side pipeline wait expired (results invalid)");
+  if (h.status)
+    return fail(MG_ERR_WORKSPACE, "workspace capacity exceeded (pairs " +
+                                      std::to_string(h.n_pairs) + ", partial items " +
+                                      std::to_string(h.n_partial_items) + ")");
+  return MG_OK;
+}
+
+int mg_flux(const float* cube, int32_t nx, int32_t ny, int32_t nc, int32_t padx, int32_t pady,
+            double* flux, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!cube || !flux || nx <= 0 || ny <= 0 || nc <= 0 || padx < 0 || pady < 0 ||
+      2 * padx >= nx || 2 * pady >= ny)
+    return fail(MG_ERR_INVALID_ARGUMENT, "invalid mg_flux arguments");
+  size_t need = sizeof(double) * (size_t)flux_chunks(nx, padx) * nc;
+  if (!workspace || workspace_bytes < need)
+    return fail(MG_ERR_WORKSPACE, "mg_flux workspace too small: need " + std::to_string(need));
+  launch_flux(cube, nx, ny, nc, padx, pady, static_cast<double*>(workspace), flux,
+              static_cast<cudaStream_t>(stream));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "mg_flux launch");
+  return MG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// mg_spectra: materialised spectra (the reference's spectral_model.spectra)
+// ---------------------------------------------------------------------------
+
+namespace mg {
+
+__global__ void k_spectra(long long n, int nc, int model, const double* __restrict__ v,
+                          const float* __restrict__ sigma, float sigma_const,
+                          const double* __restrict__ amp, const double* __restrict__ edges,
+                          float* __restrict__ out) {
+  const long long total = n * nc;
+  const int dec = edges[nc] < edges[0];
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long p = k / nc;
+    const int c = (int)(k - p * nc);
+    const double vp = v[p];
+    const double lo = dec ? edges[c + 1] : edges[c];
+    const double hi = dec ? edges[c] : edges[c + 1];
+    const float inv_w = (float)(1.0 / fabs(edges[c + 1] - edges[c]));
+    float phi;
+    if (model == MG_SPECTRUM_DIRAC) {
+      phi = (vp >= lo && vp <= hi) ? 1.f : 0.f;  // H(0) = 1 (spectral_models.py:544-570)
+    } else {
+      const double s = sigma ? (double)sigma[p] : (double)sigma_const;
+      const float is = (float)(1.0 / (1.4142135623730951 * s));
+      const float vh = (float)vp, vl = (float)(vp - (double)vh);
+      const float lh = (float)lo, ll = (float)(lo - (double)lh);
+      const float hh = (float)hi, hl = (float)(hi - (double)hh);
+      phi = half_erf_diff(((lh - vh) + (ll - vl)) * is, ((hh - vh) + (hl - vl)) * is);
+    }
+    out[k] = (float)amp[p] * phi * inv_w;
+  }
+}
+
+}  // namespace mg
+
+extern "C" int mg_spectra(const mg_problem* p, float* out, void* stream) {
+  if (!p || !out) return fail(MG_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->spectral_model != MG_SPECTRUM_GAUSSIAN && p->spectral_model != MG_SPECTRUM_DIRAC)
+    return fail(MG_ERR_INVALID_ARGUMENT, "mg_spectra needs a GAUSSIAN or DIRAC model");
+  if (p->nc <= 0 || p->n < 0 || !p->edges) return fail(MG_ERR_INVALID_ARGUMENT, "invalid problem");
+  if (p->n == 0) return MG_OK;
+  if (!p->v || !p->amp) return fail(MG_ERR_INVALID_ARGUMENT, "v and amp are required");
+  long long total = p->n * (long long)p->nc;
+  long long blocks = (total + 255) / 256;
+  if (blocks > (long long)num_sms() * 64) blocks = (long long)num_sms() * 64;
+  k_spectra<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      p->n, p->nc, p->spectral_model, p->v, p->sigma, p->sigma_const,
+      p->amp, p->edges, out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "mg_spectra launch");
+  return MG_OK;
+}

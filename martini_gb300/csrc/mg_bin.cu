@@ -1,0 +1,389 @@
+// Footprint binning: per-particle records, tile histograms, work-item plan and
+// the tile-major particle list.
+//
+// The footprint of particle p is the reference's Chebyshev-box mask
+// |i - x_p| <= r_p, |j - y_p| <= r_p (martini/martini.py:272-274) with
+// r_p = ceil(sm_length * size_in_fwhm) (martini/sph_kernels.py:257-262).
+// Its integer bounds are found here once per particle with the same FP64
+// predicate, so the set of (pixel, particle) pairs equals the reference's.
+#include <cmath>
+
+#include "mg_internal.cuh"
+
+namespace mg {
+
+// Inclusive pixel range [lo, hi] of {i : |i - c| <= r}, clipped to [0, n).
+__device__ __forceinline__ void box_bounds(double c, double r, int n, int& lo, int& hi) {
+  if (!(r >= 0.0)) {  // NaN or negative range: empty
+    lo = 0;
+    hi = -1;
+    return;
+  }
+  if (isinf(r)) {
+    lo = 0;
+    hi = n - 1;
+    return;
+  }
+  double a = floor(c - r) - 1.0;
+  double b = ceil(c + r) + 1.0;
+  if (a < 0.0) a = 0.0;
+  if (b > (double)(n - 1)) b = (double)(n - 1);
+  if (a > b) {
+    lo = 0;
+    hi = -1;
+    return;
+  }
+  int l = (int)a, h = (int)b;
+  while (l <= h && !(fabs((double)l - c) <= r)) ++l;
+  while (h >= l && !(fabs((double)h - c) <= r)) --h;
+  lo = l;
+  hi = h;
+}
+
+// Channel index range whose closed velocity interval meets [lo, hi].
+__device__ __forceinline__ void channel_range(const double* e, int nc, int dec, double lo,
+                                              double hi, int& c0, int& c1) {
+  // E(k) = edges in increasing order
+  auto E = [&](int k) { return dec ? e[nc - k] : e[k]; };
+  // first c in [0, nc) with E(c + 1) >= lo
+  int a = 0, b = nc;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    if (E(m + 1) >= lo) b = m; else a = m + 1;
+  }
+  int first = a;
+  // last c in [0, nc) with E(c) <= hi  ->  (first c with E(c) > hi) - 1
+  a = 0;
+  b = nc;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    if (E(m) > hi) b = m; else a = m + 1;
+  }
+  int last = a - 1;
+  if (first > last) {
+    c0 = 1;
+    c1 = 0;
+    return;
+  }
+  if (dec) {
+    c0 = nc - 1 - last;
+    c1 = nc - 1 - first;
+  } else {
+    c0 = first;
+    c1 = last;
+  }
+}
+
+
+// One thread per particle: exact footprint, Dirac pixel, spectral support,
+// packed record; tile histogram and per-tile channel window by atomics.
+__global__ void k_prep(PrepArgs a, Geo g, Ws w) {
+  const int dec = w.hdr->edges_dec;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    PRec rec;
+    rec.ilo = 0; rec.ihi = -1; rec.jlo = 0; rec.jhi = -1;
+    rec.clo = 1; rec.chi = 0;
+    rec.xi = rec.yi = 0;
+    rec.xf = rec.yf = 0.f;
+    rec.h = 1.f; rec.inv_h2 = 1.f;
+    rec.vhi = rec.vlo = 0.f; rec.inv_s = 0.f; rec.amp = 0.f; rec.pad_ = 0;
+    int ks = a.kidx ? (int)a.kidx[p] : 0;
+    if (ks < 0 || ks >= g.n_kernels) ks = 0;  // -1: kernels[0] (sph_kernels.py:1360)
+    rec.kslot = ks;
+    double x = a.x[p], y = a.y[p], r = a.r[p];
+    // |coordinate| > 2^30 px cannot reach the cube (and would overflow int)
+    bool ok = isfinite(x) && isfinite(y) && fabs(x) < 1073741824.0 && fabs(y) < 1073741824.0;
+    if (ok) {
+      box_bounds(x, r, g.nx, rec.ilo, rec.ihi);
+      box_bounds(y, r, g.ny, rec.jlo, rec.jhi);
+      ok = rec.ilo <= rec.ihi && rec.jlo <= rec.jhi;
+    }
+    if (ok && g.ks[ks].type == MG_KERNEL_DIRAC) {
+      // weight 1 iff |x - i| < 0.5 and |y - j| < 0.5 (sph_kernels.py:1165):
+      // at most one pixel per axis, tested in FP64.
+      int di = -1, dj = -1;
+      double fx = floor(x), fy = floor(y);
+      if (fabs(x - fx) < 0.5) di = (int)fx; else if (fabs(x - (fx + 1.0)) < 0.5) di = (int)fx + 1;
+      if (fabs(y - fy) < 0.5) dj = (int)fy; else if (fabs(y - (fy + 1.0)) < 0.5) dj = (int)fy + 1;
+      if (di < rec.ilo || di > rec.ihi || dj < rec.jlo || dj > rec.jhi) {
+        ok = false;
+      } else {
+        rec.ilo = rec.ihi = di;
+        rec.jlo = rec.jhi = dj;
+      }
+    }
+    if (ok) {
+      double fx = floor(x), fy = floor(y);
+      rec.xi = (int)fx;
+      rec.yi = (int)fy;
+      rec.xf = (float)(x - fx);
+      rec.yf = (float)(y - fy);
+      float h = a.h ? a.h[p] : 1.f;
+      rec.h = h;
+      rec.inv_h2 = 1.f / (h * h);
+      if (g.spectral_model == MG_SPECTRUM_TABLE) {
+        rec.clo = 0;
+        rec.chi = g.nc - 1;
+        rec.amp = 1.f;
+      } else {
+        double v = a.v[p];
+        double am = a.amp[p];
+        rec.amp = (float)am;
+        double vh = (double)(float)v;
+        rec.vhi = (float)vh;
+        rec.vlo = (float)(v - vh);
+        if (g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
+          double s = a.sigma ? (double)a.sigma[p] : (double)g.sigma_const;
+          rec.inv_s = (float)(1.0 / (1.4142135623730951 * s));
+          // |u| <= 6: beyond, erf differences are below 2e-17
+          double half = 6.0 * 1.4142135623730951 * s;
+          channel_range(a.edges, g.nc, dec, v - half, v + half, rec.clo, rec.chi);
+        } else {
+          channel_range(a.edges, g.nc, dec, v, v, rec.clo, rec.chi);
+        }
+        if (am == 0.0 || !isfinite(v)) {
+          rec.clo = 1;
+          rec.chi = 0;
+        }
+      }
+      ok = rec.clo <= rec.chi;
+    }
+    if (!ok) {
+      rec.ilo = 0; rec.ihi = -1; rec.jlo = 0; rec.jhi = -1;
+    }
+    w.rec[p] = rec;
+    int np = 0;
+    if (ok) {
+      int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
+      int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
+      np = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+      for (int tx = tx0; tx <= tx1; ++tx)
+        for (int ty = ty0; ty <= ty1; ++ty) {
+          int t = tx * g.nty + ty;
+          atomicAdd(&w.tile_count[t], 1);
+          atomicMin(&w.tile_wlo[t], rec.clo);
+          atomicMax(&w.tile_whi[t], rec.chi);
+        }
+      atomicMax(&w.hdr->wmax, rec.chi - rec.clo);
+      if (g.form == MG_FORM_F16X3) {
+        // magnitude bounds for the scaled FP16 split (non-negative floats
+        // order like their bit patterns)
+        const KSpec k = g.ks[ks];
+        float wb = weight_bound(k.type, rec.inv_h2, k.gnorm);
+        atomicMax(&w.hdr->wbound_bits, __float_as_uint(wb));
+        float sb = rec.amp;
+        if (g.spectral_model == MG_SPECTRUM_TABLE) {
+          sb = 0.f;
+          for (int c = 0; c < g.nc; ++c) sb = fmaxf(sb, fabsf(a.spectra[p * g.nc + c]));
+        }
+        atomicMax(&w.hdr->sbound_bits, __float_as_uint(sb));
+      }
+    }
+    w.npairs[p] = np;
+  }
+}
+
+__global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_partial) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.ntiles; t += gridDim.x * blockDim.x) {
+    w.tile_count[t] = 0;
+    w.tile_wlo[t] = 0x7fffffff;
+    w.tile_whi[t] = -1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    WsHeader* h = w.hdr;
+    h->status = 0;
+    h->item_counter = 0;
+    h->reduce_counter = 0;
+    h->edges_dec = 0;
+    h->n_pairs = h->n_items = h->n_partial_items = h->partial_bound = 0;
+    h->cap_pairs = cap_pairs;
+    h->cap_partial_items = cap_partial;
+    h->wmax = 0;
+    h->wbound_bits = 0u;
+    h->sbound_bits = 0u;
+    h->invw_bits = 0u;
+  }
+}
+
+// Single-block pass over tiles after the histogram: pair offsets of the
+// tile-major list and an upper bound on split-K partial items (every segment
+// of a tile holds at most the tile's count).
+__global__ void k_plan_tiles(Geo g, Ws w) {
+  constexpr int NT = 1024;
+  __shared__ long long s_a[NT], s_b[NT];
+  const int tid = threadIdx.x;
+  const int per = (g.ntiles + NT - 1) / NT;
+  const int t0 = tid * per;
+  const int t1 = min(g.ntiles, t0 + per);
+  long long sa = 0, sb = 0;
+  for (int t = t0; t < t1; ++t) {
+    int cnt = w.tile_count[t];
+    sa += cnt;
+    int nk = (cnt + KCH - 1) / KCH;
+    if (nk > 1) sb += (long long)nk * w.ncb_seg;
+  }
+  s_a[tid] = sa;
+  s_b[tid] = sb;
+  __syncthreads();
+  for (int off = 1; off < NT; off <<= 1) {
+    long long a = 0, b = 0;
+    if (tid >= off) { a = s_a[tid - off]; b = s_b[tid - off]; }
+    __syncthreads();
+    s_a[tid] += a;
+    s_b[tid] += b;
+    __syncthreads();
+  }
+  long long ea = s_a[tid] - sa;
+  for (int t = t0; t < t1; ++t) {
+    w.tile_off[t] = ea;
+    ea += w.tile_count[t];
+  }
+  if (tid == NT - 1) {
+    w.tile_off[g.ntiles] = s_a[NT - 1];
+    WsHeader* h = w.hdr;
+    h->n_pairs = s_a[NT - 1];
+    h->partial_bound = s_b[NT - 1];
+    unsigned st = h->status & ST_EDGES;
+    if (h->n_pairs > h->cap_pairs) st |= ST_PAIRS;
+    h->status = st;
+  }
+}
+
+// Pairs in particle order: key = tile << cbits | clo, value = particle id.
+__global__ void k_emit(long long n, Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict__ vals) {
+  if (w.hdr->status & (ST_PAIRS | ST_EDGES)) return;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const PRec rec = w.rec[p];
+    if (rec.ilo > rec.ihi) continue;
+    long long o = w.pair_off[p];
+    const int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
+    const int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
+    for (int tx = tx0; tx <= tx1; ++tx)
+      for (int ty = ty0; ty <= ty1; ++ty) {
+        const unsigned t = (unsigned)(tx * g.nty + ty);
+        keys[o] = (t << w.cbits) | (unsigned)rec.clo;
+        vals[o] = (int)p;
+        ++o;
+      }
+  }
+}
+
+// First index in [lo, hi) of sorted keys with key >= k.
+__device__ __forceinline__ long long lower_bound_keys(const unsigned* keys, long long lo,
+                                                      long long hi, unsigned k) {
+  while (lo < hi) {
+    long long m = (lo + hi) >> 1;
+    if (keys[m] < k) lo = m + 1; else hi = m;
+  }
+  return lo;
+}
+
+// One thread per segment (tile, channel block): the sorted-list range of the
+// particles whose support [clo, chi] can meet the block (clo within
+// [c0 - wmax, c0 + width)), its K chunks and its split-K partial items.
+__global__ void k_segments(Geo g, Ws w) {
+  const bool bad = (w.hdr->status & (ST_PAIRS | ST_EDGES)) != 0;
+  const int wmax = w.hdr->wmax;
+  const unsigned cmask_hi = (1u << w.cbits);
+  for (int sg = blockIdx.x * blockDim.x + threadIdx.x; sg < w.nseg; sg += gridDim.x * blockDim.x) {
+    const int t = sg / w.ncb_seg;
+    const int cb = sg - t * w.ncb_seg;
+    long long lo = w.tile_off[t], hi = w.tile_off[t + 1];
+    int items = 0, part = 0;
+    if (!bad && hi > lo) {
+      if (w.ncb_seg > 1) {
+        const int c0 = cb * w.seg_width;
+        const int clo_min = c0 - wmax > 0 ? c0 - wmax : 0;
+        const unsigned c_end = (unsigned)(c0 + w.seg_width);  // first clo past the block
+        const unsigned tk = (unsigned)t << w.cbits;
+        const long long a = lower_bound_keys(w.keys, lo, hi, tk | (unsigned)clo_min);
+        const long long b = c_end >= cmask_hi ? hi : lower_bound_keys(w.keys, a, hi, tk | c_end);
+        // skip blocks entirely outside the tile's channel window
+        if (c0 > w.tile_whi[t] || c0 + w.seg_width <= w.tile_wlo[t]) {
+          lo = hi = a;
+        } else {
+          lo = a;
+          hi = b;
+        }
+      }
+      const long long cnt = hi - lo;
+      if (cnt > 0) {
+        items = (int)((cnt + KCH - 1) / KCH);
+        part = items > 1 ? items : 0;
+      }
+    }
+    w.seg_lo[sg] = lo;
+    w.seg_hi[sg] = hi;
+    w.seg_items[sg] = items;
+    w.seg_part[sg] = part;
+  }
+}
+
+__global__ void k_check_partials(Ws w) {
+  WsHeader* h = w.hdr;
+  if (h->n_partial_items > h->cap_partial_items) h->status |= ST_PARTIALS;
+}
+
+// Channel edges as double-float pairs, inverse channel widths, edge
+// direction and the strict-monotonicity check of spectral_models.py:180-187.
+__global__ void k_edges(const double* e, int nc, Ws w) {
+  const int dec = e[nc] < e[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) w.hdr->edges_dec = dec;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= nc; k += gridDim.x * blockDim.x) {
+    double v = e[k];
+    float hi = (float)v;
+    w.ehi[k] = hi;
+    w.elo[k] = (float)(v - (double)hi);
+    if (k < nc) {
+      w.inv_w[k] = (float)(1.0 / fabs(e[k + 1] - e[k]));
+      atomicMax(&w.hdr->invw_bits, __float_as_uint(w.inv_w[k]));
+      bool mono = dec ? (e[k + 1] < e[k]) : (e[k + 1] > e[k]);
+      if (!mono) atomicOr(&w.hdr->status, ST_EDGES);
+    }
+  }
+}
+
+static unsigned grid_for(long long n, int num_sms) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > (long long)num_sms * 32) blocks = (long long)num_sms * 32;
+  return (unsigned)(blocks > 0 ? blocks : 1);
+}
+
+// Records, tile histogram, per-particle pair offsets and the tile plan.
+void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cudaStream_t s,
+                 long long cap_pairs, long long cap_partial) {
+  k_tile_init<<<(g.ntiles + 255) / 256, 256, 0, s>>>(g, w, cap_pairs, cap_partial);
+  k_edges<<<(g.nc + 256) / 256, 256, 0, s>>>(a.edges, g.nc, w);
+  if (a.n > 0) k_prep<<<grid_for(a.n, num_sms), 256, 0, s>>>(a, g, w);
+  launch_scan(w.npairs, a.n, w.pair_off, w.scan_sums, nullptr, s);
+  k_plan_tiles<<<1, 1024, 0, s>>>(g, w);
+}
+
+int sort_bits(const Geo& g, const Ws& w) {
+  int tbits = 0;
+  while ((1LL << tbits) < (long long)g.ntiles) ++tbits;
+  return tbits + w.cbits;
+}
+
+// Tile-major list sorted by (tile, clo), then the segments with their
+// work-item and partial offsets.  Pairs are emitted into the buffer from
+// which an even/odd number of radix passes ends in w.keys / w.list.
+void launch_sort_segments(const PrepArgs& a, const Geo& g, const Ws& w, long long cap_pairs,
+                          int num_sms, cudaStream_t s) {
+  const int passes = (sort_bits(g, w) + 7) / 8;
+  unsigned* k0 = (passes & 1) ? w.keys_tmp : w.keys;
+  int* v0 = (passes & 1) ? w.list_tmp : w.list;
+  unsigned* k1 = (passes & 1) ? w.keys : w.keys_tmp;
+  int* v1 = (passes & 1) ? w.list : w.list_tmp;
+  if (a.n > 0) k_emit<<<grid_for(a.n, num_sms), 256, 0, s>>>(a.n, g, w, k0, v0);
+  launch_radix_sort(k0, v0, k1, v1, &w.hdr->n_pairs, cap_pairs, sort_bits(g, w), w.rs_hist,
+                    w.rs_off, w.scan_sums, num_sms, s);
+  k_segments<<<(unsigned)((w.nseg + 255) / 256), 256, 0, s>>>(g, w);
+  launch_scan(w.seg_items, w.nseg, w.item_off, w.scan_sums, &w.hdr->n_items, s);
+  launch_scan(w.seg_part, w.nseg, w.part_off, w.scan_sums, &w.hdr->n_partial_items, s);
+  k_check_partials<<<1, 1, 0, s>>>(w);
+}
+
+}  // namespace mg

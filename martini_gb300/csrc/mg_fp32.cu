@@ -1,0 +1,254 @@
+// Plain FP32 contraction: for each work item (tile, particle chunk, channel
+// block) the CTA builds W[32 particles][128 pixels] and S[32][64 channels] in
+// shared memory and accumulates out[128][64] += W^T S on CUDA cores.
+//
+// This is the per-pixel sum of martini/martini.py:243-283 reorganised around
+// output tiles: a pixel's spectrum is the sum over the particles whose
+// footprint box contains it of weight * spectrum.
+#include "mg_internal.cuh"
+
+namespace mg {
+
+constexpr int F32_THREADS = 256;
+constexpr int F32_KC = 32;  // particles per shared-memory chunk
+
+// Segment of work item `item`: the largest sg with item_off[sg] <= item
+// (segments without items share their successor's offset).
+__device__ __forceinline__ int find_segment(const long long* item_off, int nseg, long long item) {
+  int a = 0, b = nseg;
+  while (b - a > 1) {
+    int m = (a + b) >> 1;
+    if (item_off[m] <= item) a = m; else b = m;
+  }
+  return a;
+}
+
+struct ItemInfo {
+  int seg, tile, tx, ty, kc, nk;
+  int c0;            // first channel of this item's block
+  long long lbeg;    // particle list range
+  int lcount;
+};
+
+__device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long long item) {
+  ItemInfo it;
+  const int sg = find_segment(w.item_off, w.nseg, item);
+  it.seg = sg;
+  it.tile = sg / w.ncb_seg;
+  const int cb = sg - it.tile * w.ncb_seg;
+  it.tx = it.tile / g.nty;
+  it.ty = it.tile - it.tx * g.nty;
+  it.nk = w.seg_items[sg];
+  it.kc = (int)(item - w.item_off[sg]);
+  it.c0 = cb * w.seg_width;
+  it.lbeg = w.seg_lo[sg] + (long long)it.kc * KCH;
+  const long long left = w.seg_hi[sg] - it.lbeg;
+  it.lcount = (int)(left < KCH ? left : KCH);
+  return it;
+}
+
+__global__ void __launch_bounds__(F32_THREADS, 2)
+k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict__ cube) {
+  __shared__ __align__(16) float Ws_[F32_KC][TILE_PX];
+  __shared__ __align__(16) float Ss_[F32_KC][CBLK];
+  __shared__ PRec recs[F32_KC];
+  __shared__ KSpec s_ks[MG_MAX_KERNELS];
+  __shared__ long long s_item;
+
+  const int tid = threadIdx.x;
+  if (tid < MG_MAX_KERNELS) s_ks[tid] = g.ks[tid];
+  const WsHeader* hdr = w.hdr;
+  if (hdr->status) return;
+  const long long n_items = hdr->n_items;
+  const int dec = hdr->edges_dec;
+  const int tr = tid >> 4;  // pixel group: pixels tr*8 .. tr*8+7
+  const int tc = tid & 15;  // channel group: channels tc*4 .. tc*4+3
+
+  for (;;) {
+    if (tid == 0) s_item = (long long)atomicAdd(&w.hdr->item_counter, 1u);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= n_items) break;
+    const ItemInfo it = decode_item(g, w, item);
+    const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
+
+    float acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+
+    for (int k0 = 0; k0 < it.lcount; k0 += F32_KC) {
+      const int kn = min(F32_KC, it.lcount - k0);
+      if (tid < F32_KC) {
+        if (tid < kn) {
+          int pid = w.list[it.lbeg + k0 + tid];
+          recs[tid] = w.rec[pid];
+          recs[tid].pad_ = pid;
+        } else {
+          PRec z;
+          z.ilo = 0; z.ihi = -1; z.jlo = 0; z.jhi = -1; z.clo = 1; z.chi = 0;
+          z.kslot = 0; z.pad_ = 0;
+          recs[tid] = z;
+        }
+      }
+      __syncthreads();
+      {
+        // W: particle q, tile row ii (16 pixels along j)
+        const int q = tid >> 3, ii = tid & 7;
+        const PRec r = recs[q];
+        const int i = i0 + ii;
+#pragma unroll 4
+        for (int jj = 0; jj < TILE_J; ++jj)
+          Ws_[q][ii * TILE_J + jj] = pixel_weight(r, s_ks, i, j0 + jj);
+        // S: particle q, channels c0 + ii*8 .. +7
+        for (int cc = ii * 8; cc < ii * 8 + 8; ++cc) {
+          const int c = it.c0 + cc;
+          float s = 0.f;
+          if (c < g.nc && q < kn) {
+            if (g.spectral_model == MG_SPECTRUM_TABLE) {
+              s = spectra[(long long)r.pad_ * g.nc + c];
+            } else {
+              s = channel_spectrum(r, g.spectral_model, c, dec, w.ehi, w.elo, w.inv_w);
+            }
+          }
+          Ss_[q][cc] = s;
+        }
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int k = 0; k < F32_KC; ++k) {
+        const float4 wa = *reinterpret_cast<const float4*>(&Ws_[k][tr * 8]);
+        const float4 wb = *reinterpret_cast<const float4*>(&Ws_[k][tr * 8 + 4]);
+        const float4 s = *reinterpret_cast<const float4*>(&Ss_[k][tc * 4]);
+        const float wv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          acc[a][0] = fmaf(wv[a], s.x, acc[a][0]);
+          acc[a][1] = fmaf(wv[a], s.y, acc[a][1]);
+          acc[a][2] = fmaf(wv[a], s.z, acc[a][2]);
+          acc[a][3] = fmaf(wv[a], s.w, acc[a][3]);
+        }
+      }
+      __syncthreads();
+    }
+
+    // epilogue: direct cube write (single K chunk) or split-K partial
+    if (it.nk == 1) {
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int px = tr * 8 + a;
+        const int i = i0 + px / TILE_J, j = j0 + px % TILE_J;
+        if (i >= g.nx || j >= g.ny) continue;
+        float* dst = cube + ((long long)i * g.ny + j) * g.nc;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int c = it.c0 + tc * 4 + b;
+          if (c < g.nc) dst[c] = acc[a][b];
+        }
+      }
+    } else {
+      const long long slot = w.part_off[it.seg] + it.kc;
+      float* dst = w.partial + slot * (TILE_PX * CBLK);
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int px = tr * 8 + a;
+        *reinterpret_cast<float4*>(&dst[px * CBLK + tc * 4]) =
+            make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+      }
+    }
+  }
+}
+
+// Split-K reduction: one CTA per segment with more than one K chunk; sums
+// the chunks in order (deterministic) and writes the cube block.
+__global__ void k_reduce_partials(Geo g, Ws w, float* __restrict__ cube) {
+  if (w.hdr->status) return;
+  for (int sg = blockIdx.x; sg < w.nseg; sg += gridDim.x) {
+    const int nk = w.seg_part[sg];
+    if (nk == 0) continue;
+    const int t = sg / w.ncb_seg;
+    const int cb = sg - t * w.ncb_seg;
+    const int tx = t / g.nty, ty = t - (t / g.nty) * g.nty;
+    const float* src = w.partial + w.part_off[sg] * (long long)(TILE_PX * CBLK);
+    for (int e = threadIdx.x; e < TILE_PX * CBLK; e += blockDim.x) {
+      float acc = 0.f;
+      for (int kc = 0; kc < nk; ++kc) acc += src[(long long)kc * TILE_PX * CBLK + e];
+      const int px = e / CBLK, cc = e % CBLK;
+      const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
+      const int c = cb * CBLK + cc;
+      if (i < g.nx && j < g.ny && c < g.nc) cube[((long long)i * g.ny + j) * g.nc + c] = acc;
+    }
+  }
+}
+
+// FP64 flux sums over the unpadded region: per-chunk partials, then a
+// fixed-order final reduction (martini/martini.py:367-392).
+constexpr int FLUX_ROWS = 8;  // pixel rows (axis 0) per chunk
+
+__global__ void k_flux_partial(const float* __restrict__ cube, int nx, int ny, int nc, int padx,
+                               int pady, double* __restrict__ part) {
+  const int chunk = blockIdx.x;
+  const int i0 = padx + chunk * FLUX_ROWS;
+  const int i1 = min(nx - padx, i0 + FLUX_ROWS);
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    double acc = 0.0;
+    for (int i = i0; i < i1; ++i) {
+      const float* row = cube + ((long long)i * ny) * nc + c;
+      float f = 0.f;
+      int cnt = 0;
+      for (int j = pady; j < ny - pady; ++j) {
+        f += row[(long long)j * nc];
+        if (++cnt == 8) {
+          acc += (double)f;
+          f = 0.f;
+          cnt = 0;
+        }
+      }
+      acc += (double)f;
+    }
+    part[(long long)chunk * nc + c] = acc;
+  }
+}
+
+__global__ void k_flux_final(const double* __restrict__ part, int nchunks, int nc,
+                             double* __restrict__ flux) {
+  __shared__ double red[1024];
+  double tot = 0.0;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < nchunks; ++k) s += part[(long long)k * nc + c];
+    flux[1 + c] = s;
+    tot += s;
+  }
+  red[threadIdx.x] = tot;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) flux[0] = red[0];
+}
+
+int flux_chunks(int nx, int padx) {
+  int rows = nx - 2 * padx;
+  if (rows < 1) rows = 1;
+  return (rows + FLUX_ROWS - 1) / FLUX_ROWS;
+}
+
+void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, double* part,
+                 double* flux, cudaStream_t s) {
+  const int nch = flux_chunks(nx, padx);
+  const int thr = nc < 256 ? ((nc + 31) / 32) * 32 : 256;
+  k_flux_partial<<<nch, thr, 0, s>>>(cube, nx, ny, nc, padx, pady, part);
+  k_flux_final<<<1, 1024, 0, s>>>(part, nch, nc, flux);
+}
+
+void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
+                          int num_sms, cudaStream_t s) {
+  k_contract_fp32<<<num_sms * 2, F32_THREADS, 0, s>>>(g, w, spectra, cube);
+  k_reduce_partials<<<num_sms * 8, 256, 0, s>>>(g, w, cube);
+}
+
+}  // namespace mg

@@ -1,0 +1,257 @@
+// Internal device-side definitions shared by the martini_gb300 kernels.
+//
+// Cube tiles are TILE_I x TILE_J pixels (128 pixels: one tensor-core M tile)
+// and contraction channel blocks are CBLK channels.  Particles are binned by
+// the tiles their footprint box touches; each (tile, particle-chunk,
+// channel-block) is one work item of the contraction kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/martini_gb300.h"
+#include "mg_kernel_tables.h"
+
+namespace mg {
+
+constexpr int TILE_I = 8;    // pixels along axis 0 (RA index)
+constexpr int TILE_J = 16;   // pixels along axis 1 (Dec index)
+constexpr int TILE_PX = TILE_I * TILE_J;
+constexpr int CBLK = 64;     // channels per FP32 work item
+constexpr int KCH = 2048;    // particles per work item (split-K granularity)
+
+// Per-particle record written by the prep kernel (64 bytes).
+struct PRec {
+  int ilo, ihi, jlo, jhi;  // exact footprint box (inclusive), clipped; empty if ilo > ihi
+  int xi, yi;              // floor(x), floor(y)
+  float xf, yf;            // x - xi, y - yi in [0, 1)
+  float h;                 // sm_length * rescale, px
+  float inv_h2;            // 1 / h^2
+  int kslot;               // resolved kernel table slot
+  int clo, chi;            // channel support, inclusive; empty if clo > chi
+  float vhi, vlo;          // velocity as a double-float pair, km/s
+  float inv_s;             // 1 / (sqrt(2) sigma), km/s^-1
+  float amp;               // mHI / D^2 / 2.36e5
+  int pad_;
+};
+
+struct KSpec {
+  int type;
+  float truncate;
+  float gnorm;       // Gaussian truncation normalisation
+  float pad_;
+};
+
+// Device-side problem constants (copied into kernel parameters).
+struct Geo {
+  int nx, ny, nc;
+  int padx, pady;
+  int ntx, nty, ntiles;
+  int n_kernels;
+  int spectral_model;
+  float sigma_const;
+  int form;
+  KSpec ks[MG_MAX_KERNELS];
+};
+
+// Status bits of WsHeader::status.
+constexpr unsigned ST_PAIRS = 1u;        // pairs exceed the list capacity
+constexpr unsigned ST_PARTIALS = 2u;     // split-K partials exceed capacity
+constexpr unsigned ST_EDGES = 4u;        // channel edges not strictly monotonic
+constexpr unsigned ST_TIMEOUT = 8u;      // a bounded device-side wait expired
+
+// Workspace header (device): status flags and scalar counters.
+struct WsHeader {
+  unsigned int status;           // ST_* bits
+  unsigned int item_counter;     // dynamic scheduler cursor
+  unsigned int reduce_counter;
+  int edges_dec;                 // 1 if channel edges decrease with index
+  long long n_pairs;
+  long long n_items;
+  long long n_partial_items;
+  long long partial_bound;       // upper bound on partial items (from tile counts)
+  long long cap_pairs;
+  long long cap_partial_items;
+  int wmax;                      // max (chi - clo) over particles
+  unsigned wbound_bits;          // max pixel weight bound (float bits, >= 0)
+  unsigned sbound_bits;          // max spectrum bound (float bits, >= 0)
+  unsigned invw_bits;            // max 1 / |channel width| (float bits)
+  long long pad1[4];
+};
+
+// Pointers into the workspace (host computes, passes by value).  A
+// "segment" is one (tile, channel block) of the contraction: ncb_seg blocks
+// per tile (FP32 form: ceil(nc / CBLK); tensor-core form: 1, the full band).
+struct Ws {
+  WsHeader* hdr;
+  PRec* rec;             // [n]
+  int* npairs;           // [n] tiles touched per particle
+  long long* pair_off;   // [n] exclusive scan of npairs
+  int* tile_count;       // [ntiles]
+  int* tile_wlo;         // [ntiles]
+  int* tile_whi;         // [ntiles]
+  long long* tile_off;   // [ntiles + 1] pair offsets (tile-major sorted list)
+  float* ehi;            // [nc + 1] edges, double-float high part
+  float* elo;            // [nc + 1] low part
+  float* inv_w;          // [nc] 1 / |channel width|
+  unsigned* keys;        // [cap_pairs] sorted keys: tile << cbits | clo
+  int* list;             // [cap_pairs] particle ids in sorted order
+  unsigned* keys_tmp;    // [cap_pairs] radix-sort second buffer
+  int* list_tmp;         // [cap_pairs]
+  int* rs_hist;          // [256 * radix_blocks(cap_pairs)]
+  long long* rs_off;     // [256 * radix_blocks(cap_pairs)]
+  long long* scan_sums;  // [scan scratch]
+  long long* seg_lo;     // [nseg] list range of each segment
+  long long* seg_hi;     // [nseg]
+  int* seg_items;        // [nseg] work items (K chunks) of each segment
+  int* seg_part;         // [nseg] partial items of each segment
+  long long* item_off;   // [nseg] exclusive scan of seg_items
+  long long* part_off;   // [nseg] exclusive scan of seg_part
+  float* partial;        // [cap_partial_items][TILE_PX][seg_width]
+  double* flux_part;     // [flux_chunks][nc]
+  int nseg;              // ntiles * ncb_seg
+  int ncb_seg;           // channel blocks per tile
+  int seg_width;         // channels per segment (CBLK or nc rounded up to 16)
+  int cbits;             // channel bits of the sort key
+};
+
+// Particle inputs of the prep kernel (device pointers from mg_problem).
+struct PrepArgs {
+  long long n;
+  const double* x;
+  const double* y;
+  const double* r;
+  const float* h;
+  const int8_t* kidx;
+  const double* v;
+  const float* sigma;
+  const double* amp;
+  const double* edges;
+  const float* spectra;
+};
+
+// Host-side launchers.
+void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cudaStream_t s,
+                 long long cap_pairs, long long cap_partial);
+void launch_sort_segments(const PrepArgs& a, const Geo& g, const Ws& w, long long cap_pairs,
+                          int num_sms, cudaStream_t s);
+int sort_bits(const Geo& g, const Ws& w);
+void launch_scan(const int* in, long long n, long long* out, long long* sums, long long* total,
+                 cudaStream_t s);
+long long scan_blocks(long long n);
+long long radix_blocks(long long n);
+bool launch_radix_sort(unsigned* keys, int* vals, unsigned* kt, int* vt, const long long* np,
+                       long long cap, int bits, int* hist, long long* off, long long* sums,
+                       int num_sms, cudaStream_t s);
+void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
+                          int num_sms, cudaStream_t s);
+int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
+                           int num_sms, cudaStream_t s);
+void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, double* part,
+                 double* flux, cudaStream_t s);
+int flux_chunks(int nx, int padx);
+
+// ---------------------------------------------------------------------------
+// Kernel pixel integrals (martini/sph_kernels.py).  dx, dy are particle minus
+// pixel centre in px, h the rescaled smoothing length.  Each returns the
+// integral over the pixel per unit pixel area (px^-2).
+// ---------------------------------------------------------------------------
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// Radial kernels (WendlandC2 sph_kernels.py:400-441, WendlandC6 :544-685,
+// cubic spline :791-858, quartic spline :1486-1564): the pixel integral is
+// scale * f(s) / h^2 with s = R^2 (offsets doubled for the cubic spline).
+// f comes from degree-7 polynomials on uniform cells fitted in FP64 to the
+// reference closed forms (mg_kernel_tables.h, made by gen_kernel_tables.py):
+// a direct cell index and one Horner sweep, accurate to ~1e-7 of f(0) in
+// FP32 where the closed forms lose up to 7e-4.
+__device__ __forceinline__ float kt_eval(int kt, float s) {
+  const KTableInfo& inf = kt_info[kt];
+  if (!(s < inf.smax)) return 0.f;
+  const float R = sqrtf(s);
+  int r = 0;
+  if (inf.nreg == 3) r = (s > 1.f) ? 2 : (R >= inf.split_r ? 1 : 0);
+  const KRegion g = inf.reg[r];
+  const float v = g.var ? sqrtf(fmaxf(1.f - s, 0.f)) : R;
+  const float u = (v - g.lo) * g.cells_per_unit;
+  int c = (int)u;
+  c = c < 0 ? 0 : (c >= g.ncell ? g.ncell - 1 : c);
+  const float t = u - (float)c;
+  const float4* c4 = reinterpret_cast<const float4*>(kt_coef) + 2 * (g.first + c);
+  const float4 lo = __ldg(c4), hi = __ldg(c4 + 1);
+  float acc = hi.w;
+  acc = fmaf(acc, t, hi.z);
+  acc = fmaf(acc, t, hi.y);
+  acc = fmaf(acc, t, hi.x);
+  acc = fmaf(acc, t, lo.w);
+  acc = fmaf(acc, t, lo.z);
+  acc = fmaf(acc, t, lo.y);
+  return fmaf(acc, t, lo.x);
+}
+
+__device__ __forceinline__ float w_radial(int kt, float r2, float inv_h2) {
+  const float s = (kt == MG_KERNEL_CUBIC_SPLINE ? 4.f : 1.f) * r2 * inv_h2;
+  return kt_eval(kt, s) * kt_info[kt].scale * inv_h2;
+}
+
+// Upper bound of a particle's pixel weight (per unit pixel area).
+__device__ __forceinline__ float weight_bound(int type, float inv_h2, float gnorm) {
+  if (type == MG_KERNEL_DIRAC) return 1.f;
+  if (type == MG_KERNEL_GAUSSIAN) return 1.f / gnorm;
+  return kt_eval(type, 0.f) * kt_info[type].scale * inv_h2;
+}
+
+// _GaussianKernel._kernel_integral, sph_kernels.py:994-1044.
+__device__ __forceinline__ float w_gaussian(float dx, float dy, float h, float trunc,
+                                            float gnorm) {
+  const float sig = 0.42466090014400953f;  // 1 / (2 sqrt(2 ln 2))
+  float dr = sqrtf(dx * dx + dy * dy);
+  float q = dr / h / sig;
+  if ((dr - 0.70710678118654752f) / h / sig > trunc) return 0.f;
+  float zmax = trunc > q ? sqrtf(trunc * trunc - q * q) : 0.f;
+  float s = 1.f / (h * 1.41421356237309505f * sig);
+  float ex = erff((dx + 0.5f) * s) - erff((dx - 0.5f) * s);
+  float ey = erff((dy + 0.5f) * s) - erff((dy - 0.5f) * s);
+  return 0.25f * erff(zmax * 0.70710678118654752f) * ex * ey / gnorm;
+}
+
+// Weight of pixel (i, j) for a particle record; 0 outside the footprint box.
+__device__ __forceinline__ float pixel_weight(const PRec& r, const KSpec* ks, int i, int j) {
+  if (i < r.ilo || i > r.ihi || j < r.jlo || j > r.jhi) return 0.f;
+  const KSpec k = ks[r.kslot];
+  if (k.type == MG_KERNEL_DIRAC) return 1.f;  // footprint reduced to the one pixel
+  float dx = (float)(r.xi - i) + r.xf;
+  float dy = (float)(r.yi - j) + r.yf;
+  float r2 = dx * dx + dy * dy;
+  if (k.type == MG_KERNEL_GAUSSIAN) return w_gaussian(dx, dy, r.h, k.truncate, k.gnorm);
+  return w_radial(k.type, r2, r.inv_h2);
+}
+
+// ---------------------------------------------------------------------------
+// Channel spectra (martini/spectral_models.py)
+// ---------------------------------------------------------------------------
+
+// 0.5 [erf(b) - erf(a)] for b >= a, using erfc in the tails.
+__device__ __forceinline__ float half_erf_diff(float a, float b) {
+  if (a >= 0.f) return 0.5f * (erfcf(a) - erfcf(b));
+  if (b <= 0.f) return 0.5f * (erfcf(-b) - erfcf(-a));
+  return 0.5f * (erff(b) - erff(a));
+}
+
+// S_p(c) for one channel (GAUSSIAN / DIRAC), spectral_models.py:63-200.
+// Edge e of the cube is (ehi[e] + elo[e]); the channel's lower/upper edges
+// depend on the edge direction (spectral_models.py:180-187).
+__device__ __forceinline__ float channel_spectrum(const PRec& r, int model, int c, int dec,
+                                                  const float* ehi, const float* elo,
+                                                  const float* inv_w) {
+  if (c < r.clo || c > r.chi) return 0.f;
+  if (model == MG_SPECTRUM_DIRAC) return r.amp * inv_w[c];
+  int e_lo = dec ? c + 1 : c;
+  int e_hi = dec ? c : c + 1;
+  float a = ((ehi[e_lo] - r.vhi) + (elo[e_lo] - r.vlo)) * r.inv_s;
+  float b = ((ehi[e_hi] - r.vhi) + (elo[e_hi] - r.vlo)) * r.inv_s;
+  return r.amp * half_erf_diff(a, b) * inv_w[c];
+}
+
+}  // namespace mg

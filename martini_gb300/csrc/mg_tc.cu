@@ -1,0 +1,614 @@
+// Split-precision tensor-core contraction (tcgen05, sm_103a).
+//
+// One persistent CTA (16 warps) per SM walks the work items (tile, K chunk).
+// For each stage of KC particles of the tile's (tile, clo)-sorted list the
+// 512 threads build in shared memory
+//   A = W[128 pixels][KC particles]        (kernel pixel integrals)
+//   B = S[Nw channels][KC particles]       (spectra over the stage's window)
+// each split into a hi + lo pair of 16-bit floats (bf16, or fp16 after exact
+// power-of-two scaling), stored K-major in the no-swizzle canonical layout
+// (8-row x 16-byte core matrices; K-direction stride 128 B, row-group stride
+// 256 B).  Thread 0 issues three tcgen05.mma (kind::f16, FP32 accumulate) per
+// 16-particle step -- W_hi S_hi + W_hi S_lo + W_lo S_hi -- into a TMEM
+// accumulator holding the tile's whole band (128 lanes = pixels, columns =
+// channels), at the stage's column window.  Two shared-memory stages
+// alternate: producers fill one while the tensor core reads the other, and
+// tcgen05.commit arrives on the stage's mbarrier when it may be reused.  The
+// records of the next stage are fetched while the current one is produced.
+// The epilogue reads TMEM with tcgen05.ld and writes 128-byte channel runs
+// of each pixel to the cube, or to a split-K partial buffer.
+//
+// Every mbarrier wait has an iteration limit: on expiry the kernel sets
+// ST_TIMEOUT, frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "mg_internal.cuh"
+
+namespace mg {
+
+constexpr int TC_THREADS = 512;
+constexpr int TC_TMEM_COLS = 512;  // whole TMEM: one CTA per SM
+constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
+// The tensor core's FP32 accumulation does not round to nearest: summing
+// many MMAs into one accumulator drifts low (~2^-26 per MMA, relative).  When
+// the band fits in half of TMEM the working accumulator is drained every
+// TC_DRAIN stages into a master accumulator in the other half with
+// round-to-nearest FP32 adds, which bounds that drift to ~TC_DRAIN * 3 * KC/16
+// MMAs per partial sum.
+constexpr int TC_DRAIN = 2;
+constexpr int TC_MASTER_COL = 256;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (unsigned i = 0; i < TC_SPIN_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, no swizzle (layout type 0),
+// descriptor version 1; lbo = byte stride between the two K core matrices,
+// sbo = byte stride between 8-row groups.
+__device__ __forceinline__ unsigned long long sdesc(unsigned saddr, unsigned lbo, unsigned sbo) {
+  unsigned long long d = 0;
+  d |= (unsigned long long)((saddr & 0x3FFFFu) >> 4);
+  d |= (unsigned long long)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (unsigned long long)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= 1ull << 46;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D FP32; A, B both BF16 (format 1) or
+// both FP16 (format 0); both K-major; N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ unsigned idesc_f16kind(int M, int N, bool bf16) {
+  const unsigned fmt = bf16 ? 1u : 0u;
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((unsigned)(N >> 3) << 17) |
+         ((unsigned)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(unsigned d_tmem, unsigned long long a, unsigned long long b,
+                                     unsigned idesc, unsigned acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(unsigned bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_st32_zero(unsigned taddr) {
+  const unsigned z = 0u;
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+      "%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+      "%1};" ::"r"(taddr),
+      "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15])
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// hi + lo split of a float into two 16-bit floats.
+template <bool BF16>
+__device__ __forceinline__ void split2(float v, unsigned short& hi, unsigned short& lo) {
+  if (BF16) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    hi = __bfloat16_as_ushort(h);
+    lo = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h)));
+  } else {
+    const __half h = __float2half_rn(v);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__float2half_rn(v - __half2float(h)));
+  }
+}
+
+template <bool BF16>
+__device__ __forceinline__ void store8(unsigned char* hi_base, unsigned char* lo_base,
+                                       unsigned off, const float (&v)[8]) {
+  unsigned short h[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) split2<BF16>(v[e], h[e], l[e]);
+  *reinterpret_cast<uint4*>(hi_base + off) =
+      make_uint4(h[0] | ((unsigned)h[1] << 16), h[2] | ((unsigned)h[3] << 16),
+                 h[4] | ((unsigned)h[5] << 16), h[6] | ((unsigned)h[7] << 16));
+  *reinterpret_cast<uint4*>(lo_base + off) =
+      make_uint4(l[0] | ((unsigned)l[1] << 16), l[2] | ((unsigned)l[3] << 16),
+                 l[4] | ((unsigned)l[5] << 16), l[6] | ((unsigned)l[7] << 16));
+}
+
+// Spectrum of one channel for the tensor-core producers (GAUSSIAN: the
+// erf difference across the channel, with erfc in the tails so that the
+// far wings of many lines do not accumulate cancellation error; DIRAC; TABLE).
+__device__ __forceinline__ float tc_spectrum(const PRec& r, int model, int c, int dec,
+                                             const float* ehi, const float* elo,
+                                             const float* inv_w, const float* spectra, int pid,
+                                             int nc) {
+  if (c < r.clo || c > r.chi) return 0.f;
+  if (model == MG_SPECTRUM_TABLE) return spectra[(long long)pid * nc + c];
+  const float iw = inv_w[c];
+  if (model == MG_SPECTRUM_DIRAC) return r.amp * iw;
+  const int e0 = dec ? c + 1 : c;  // lower edge
+  const int e1 = dec ? c : c + 1;  // upper edge
+  const float a = ((ehi[e0] - r.vhi) + (elo[e0] - r.vlo)) * r.inv_s;
+  const float b = ((ehi[e1] - r.vhi) + (elo[e1] - r.vlo)) * r.inv_s;
+  return r.amp * half_erf_diff(a, b) * iw;
+}
+
+struct ItemTC {
+  int tile, tx, ty, kc, nk;
+  long long lbeg;
+  int lcount;
+};
+
+__device__ __forceinline__ ItemTC decode_tc(const Geo& g, const Ws& w, long long item) {
+  int a = 0, b = w.nseg;
+  while (b - a > 1) {
+    int m = (a + b) >> 1;
+    if (w.item_off[m] <= item) a = m; else b = m;
+  }
+  ItemTC it;
+  it.tile = a;  // one segment per tile in this form
+  it.tx = a / g.nty;
+  it.ty = a - it.tx * g.nty;
+  it.nk = w.seg_items[a];
+  it.kc = (int)(item - w.item_off[a]);
+  it.lbeg = w.seg_lo[a] + (long long)it.kc * KCH;
+  const long long left = w.seg_hi[a] - it.lbeg;
+  it.lcount = (int)(left < KCH ? left : KCH);
+  return it;
+}
+
+__device__ __forceinline__ PRec empty_rec() {
+  PRec z;
+  z.ilo = 0; z.ihi = -1; z.jlo = 0; z.jhi = -1; z.clo = 1; z.chi = 0;
+  z.kslot = 0; z.xi = z.yi = 0; z.xf = z.yf = 0.f; z.h = 1.f; z.inv_h2 = 1.f;
+  z.vhi = z.vlo = 0.f; z.inv_s = 0.f; z.amp = 0.f; z.pad_ = 0;
+  return z;
+}
+
+template <bool BF16, int KC>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict__ cube,
+              int nwmax) {
+  constexpr int KSTEPS = KC / 16;
+  constexpr int GROUPS = KC / 8;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ PRec recs[2][KC];
+  __shared__ int s_pid[2][KC];
+  __shared__ KSpec s_ks[MG_MAX_KERNELS];
+  __shared__ __align__(8) unsigned long long bars[2];
+  __shared__ unsigned s_tmem;
+  __shared__ long long s_item;
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  if (w.hdr->status) return;
+  const long long n_items = w.hdr->n_items;
+  const int dec = w.hdr->edges_dec;
+
+  // exact power-of-two operand scales (FP16 form): largest |W|, |S| -> 2^14
+  float sw = 1.f, ss = 1.f;
+  if (!BF16) {
+    const float wb = __uint_as_float(w.hdr->wbound_bits);
+    const float sb = __uint_as_float(w.hdr->sbound_bits) *
+                     (g.spectral_model == MG_SPECTRUM_TABLE ? 1.f
+                                                            : __uint_as_float(w.hdr->invw_bits));
+    if (wb > 0.f) sw = exp2f(14.f - ceilf(log2f(wb)));
+    if (sb > 0.f) ss = exp2f(14.f - ceilf(log2f(sb)));
+  }
+  const float unscale = 1.f / (sw * ss);
+
+  const unsigned a_bytes = KSTEPS * 4096u;
+  const unsigned b_bytes = KSTEPS * (unsigned)nwmax * 32u;
+  const unsigned st_bytes = 2u * a_bytes + 2u * b_bytes;
+  const unsigned sbase = smem_u32(smem);
+
+  if (tid < MG_MAX_KERNELS) s_ks[tid] = g.ks[tid];
+  if (tid == 0) {
+    mbar_init(smem_u32(&bars[0]), 1);
+    mbar_init(smem_u32(&bars[1]), 1);
+    s_abort = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&s_tmem)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = s_tmem;
+  const int quarter = warp & 3;    // TMEM lane quarter of this warp
+  const int colgrp = warp >> 2;    // 4 warps share a quarter: 32-column groups
+  const unsigned lane_base = (unsigned)(quarter * 32) << 16;
+  const int ncols = w.seg_width;   // channels held in TMEM (nc rounded to 16)
+
+  const bool drain = ncols <= TC_MASTER_COL;  // master accumulator fits
+  auto zero_tmem = [&]() {
+    for (int c = colgrp * 32; c < ncols; c += 128) {
+      tmem_st32_zero(tmem + lane_base + c);
+      if (drain) tmem_st32_zero(tmem + lane_base + TC_MASTER_COL + c);
+    }
+    tmem_wait_st();
+  };
+  // master += working (round to nearest), working = 0; no MMA in flight
+  auto drain_tmem = [&]() {
+    for (int c = colgrp * 32; c < ncols; c += 128) {
+      for (int h = 0; h < 32; h += 16) {
+        unsigned a[16], b[16];
+        tmem_ld16(tmem + lane_base + c + h, a);
+        tmem_ld16(tmem + lane_base + TC_MASTER_COL + c + h, b);
+        tmem_wait_ld();
+#pragma unroll
+        for (int v = 0; v < 16; ++v) {
+          b[v] = __float_as_uint(__uint_as_float(a[v]) + __uint_as_float(b[v]));
+          a[v] = 0u;
+        }
+        tmem_st16(tmem + lane_base + TC_MASTER_COL + c + h, b);
+        tmem_st16(tmem + lane_base + c + h, a);
+      }
+    }
+    tmem_wait_st();
+  };
+  zero_tmem();
+  tc_fence_before();
+  __syncthreads();
+
+  unsigned phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  int stage = 0;
+  int since_drain = 0;
+
+  for (;;) {
+    if (tid == 0) s_item = (long long)atomicAdd(&w.hdr->item_counter, 1u);
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= n_items || s_abort) break;
+    const ItemTC it = decode_tc(g, w, item);
+    const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
+    const int nchunk = (it.lcount + KC - 1) / KC;
+
+    // records of the first stage
+    if (tid < KC) {
+      if (tid < it.lcount) {
+        const int pid = w.list[it.lbeg + tid];
+        recs[0][tid] = w.rec[pid];
+        s_pid[0][tid] = pid;
+      } else {
+        recs[0][tid] = empty_rec();
+        s_pid[0][tid] = 0;
+      }
+    }
+    __syncthreads();
+
+    for (int ch = 0; ch < nchunk; ++ch) {
+      const int buf = ch & 1;
+      const int k0 = ch * KC;
+      const int kn = min(KC, it.lcount - k0);
+      // the stage must be free: every thread waits for the MMAs that last read it
+      if (pending[stage]) {
+        if (!mbar_wait(smem_u32(&bars[stage]), phase[stage])) s_abort = 1;
+        phase[stage] ^= 1u;
+        pending[stage] = false;
+      }
+      // fetch the next stage's records while this one is produced
+      PRec nrec;
+      int npid = 0;
+      const bool has_next = ch + 1 < nchunk;
+      if (has_next && tid < KC) {
+        if (k0 + KC + tid < it.lcount) {
+          npid = w.list[it.lbeg + k0 + KC + tid];
+          nrec = w.rec[npid];
+        } else {
+          nrec = empty_rec();
+        }
+      }
+      // stage channel window [w0, w0 + nw): min clo, max chi (every warp)
+      int w0, nw;
+      {
+        int lo = 0x7fffffff, hi = -1;
+        for (int q = lane; q < kn; q += 32) {
+          lo = min(lo, recs[buf][q].clo);
+          hi = max(hi, recs[buf][q].chi);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+          hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        w0 = lo & ~15;
+        nw = ((hi + 1 - w0) + 15) & ~15;
+        if (nw < 16) nw = 16;
+        if (nw > nwmax) nw = nwmax;
+        if (w0 + nw > ncols) w0 = ncols - nw;
+        if (w0 < 0) w0 = 0;
+      }
+      unsigned char* const sa_hi = smem + stage * st_bytes;
+      unsigned char* const sa_lo = sa_hi + a_bytes;
+      unsigned char* const sb_hi = sa_lo + a_bytes;
+      unsigned char* const sb_lo = sb_hi + b_bytes;
+      // ---- A = W: task (pixel p, particle group q8): 8 values, 16 bytes
+      for (int task = tid; task < TILE_PX * GROUPS; task += TC_THREADS) {
+        const int p = task & (TILE_PX - 1);
+        const int q8 = task >> 7;
+        const int i = i0 + p / TILE_J, j = j0 + p % TILE_J;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) v[e] = pixel_weight(recs[buf][q8 * 8 + e], s_ks, i, j) * sw;
+        const unsigned off =
+            (q8 >> 1) * 4096u + (unsigned)(p >> 3) * 256u + (q8 & 1) * 128u + (p & 7) * 16u;
+        store8<BF16>(sa_hi, sa_lo, off, v);
+      }
+      // ---- B = S: task (channel n of the window, particle group q8)
+      for (int task = tid; task < nw * GROUPS; task += TC_THREADS) {
+        const int n = task % nw;
+        const int q8 = task / nw;
+        const int c = w0 + n;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int q = q8 * 8 + e;
+          v[e] = (c < g.nc && q < kn)
+                     ? tc_spectrum(recs[buf][q], g.spectral_model, c, dec, w.ehi, w.elo,
+                                   w.inv_w, spectra, s_pid[buf][q], g.nc) * ss
+                     : 0.f;
+        }
+        const unsigned off = (q8 >> 1) * ((unsigned)nw * 32u) + (unsigned)(n >> 3) * 256u +
+                             (q8 & 1) * 128u + (n & 7) * 16u;
+        store8<BF16>(sb_hi, sb_lo, off, v);
+      }
+      if (has_next && tid < KC) {
+        recs[buf ^ 1][tid] = nrec;
+        s_pid[buf ^ 1][tid] = npid;
+      }
+      fence_proxy_async();
+      __syncthreads();
+      if (s_abort) break;
+      if (tid == 0) {
+        tc_fence_after();
+        const unsigned base = sbase + stage * st_bytes;
+        for (int ks = 0; ks < KSTEPS; ++ks) {
+          const unsigned a_hi = base + ks * 4096u;
+          const unsigned a_lo = a_hi + a_bytes;
+          for (int n0 = 0; n0 < nw; n0 += 256) {
+            const int pn = nw - n0 < 256 ? nw - n0 : 256;
+            const unsigned boff = ks * ((unsigned)nw * 32u) + (unsigned)(n0 >> 3) * 256u;
+            const unsigned b_hi = base + 2u * a_bytes + boff;
+            const unsigned b_lo = b_hi + b_bytes;
+            const unsigned d = tmem + (unsigned)(w0 + n0);
+            const unsigned id = idesc_f16kind(128, pn, BF16);
+            umma(d, sdesc(a_hi, 128, 256), sdesc(b_hi, 128, 256), id, 1u);
+            umma(d, sdesc(a_hi, 128, 256), sdesc(b_lo, 128, 256), id, 1u);
+            umma(d, sdesc(a_lo, 128, 256), sdesc(b_hi, 128, 256), id, 1u);
+          }
+        }
+        umma_commit(smem_u32(&bars[stage]));
+      }
+      pending[stage] = true;
+      stage ^= 1;
+      if (drain && ++since_drain == TC_DRAIN && ch + 1 < nchunk) {
+        // wait for this stage's MMAs (the commit covers all earlier ones)
+        const int s = stage ^ 1;
+        if (!mbar_wait(smem_u32(&bars[s]), phase[s])) s_abort = 1;
+        phase[s] ^= 1u;
+        pending[s] = false;
+        tc_fence_after();
+        drain_tmem();
+        tc_fence_before();
+        __syncthreads();
+        since_drain = 0;
+        if (s_abort) break;
+      }
+    }
+    since_drain = 0;
+
+    // all MMAs of the item complete (a commit covers every earlier MMA)
+    for (int s = 0; s < 2; ++s) {
+      if (pending[s]) {
+        if (!mbar_wait(smem_u32(&bars[s]), phase[s])) s_abort = 1;
+        phase[s] ^= 1u;
+        pending[s] = false;
+      }
+    }
+    __syncthreads();
+    if (s_abort) {
+      if (tid == 0) atomicOr(&w.hdr->status, ST_TIMEOUT);
+      break;
+    }
+    tc_fence_after();
+    // ---- epilogue: TMEM -> registers -> cube or partial
+    {
+      const int p = quarter * 32 + lane;
+      const int i = i0 + p / TILE_J, j = j0 + p % TILE_J;
+      const bool inside = i < g.nx && j < g.ny;
+      float* dst;
+      int limit;
+      if (it.nk == 1) {
+        dst = cube + ((long long)i * g.ny + j) * g.nc;
+        limit = g.nc;
+      } else {
+        const long long slot = w.part_off[it.tile] + it.kc;
+        dst = w.partial + (slot * TILE_PX + p) * (long long)ncols;
+        limit = ncols;
+      }
+      const bool vec = ((limit & 3) == 0);
+      for (int c = colgrp * 32; c < ncols; c += 128) {
+        unsigned r[32];
+        tmem_ld32(tmem + lane_base + (unsigned)c, r);
+        tmem_wait_ld();
+        if (drain) {
+          for (int h = 0; h < 32; h += 16) {
+            unsigned m[16];
+            tmem_ld16(tmem + lane_base + TC_MASTER_COL + (unsigned)(c + h), m);
+            tmem_wait_ld();
+#pragma unroll
+            for (int v = 0; v < 16; ++v)
+              r[h + v] = __float_as_uint(__uint_as_float(r[h + v]) + __uint_as_float(m[v]));
+          }
+        }
+        if (inside || it.nk != 1) {
+          if (vec && c + 32 <= limit) {
+#pragma unroll
+            for (int v = 0; v < 8; ++v)
+              *reinterpret_cast<float4*>(dst + c + 4 * v) = make_float4(
+                  __uint_as_float(r[4 * v]) * unscale, __uint_as_float(r[4 * v + 1]) * unscale,
+                  __uint_as_float(r[4 * v + 2]) * unscale,
+                  __uint_as_float(r[4 * v + 3]) * unscale);
+          } else {
+#pragma unroll
+            for (int v = 0; v < 32; ++v)
+              if (c + v < limit) dst[c + v] = __uint_as_float(r[v]) * unscale;
+          }
+        }
+      }
+    }
+    zero_tmem();
+    tc_fence_before();
+    __syncthreads();
+  }
+
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// Split-K reduction for the tensor-core forms (full-band partial rows).
+__global__ void k_reduce_partials_tc(Geo g, Ws w, float* __restrict__ cube) {
+  if (w.hdr->status) return;
+  const int width = w.seg_width;
+  for (int t = blockIdx.x; t < w.nseg; t += gridDim.x) {
+    const int nk = w.seg_part[t];
+    if (nk == 0) continue;
+    const int tx = t / g.nty, ty = t - (t / g.nty) * g.nty;
+    const float* src = w.partial + w.part_off[t] * (long long)(TILE_PX * width);
+    for (int e = threadIdx.x; e < TILE_PX * width; e += blockDim.x) {
+      float acc = 0.f;
+      for (int kc = 0; kc < nk; ++kc) acc += src[(long long)kc * TILE_PX * width + e];
+      const int px = e / width, c = e % width;
+      const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
+      if (i < g.nx && j < g.ny && c < g.nc) cube[((long long)i * g.ny + j) * g.nc + c] = acc;
+    }
+  }
+}
+
+template <bool BF16, int KC>
+int launch_tc(const Geo& g, const Ws& w, const float* spectra, float* cube, int num_sms,
+              cudaStream_t s, int nwmax) {
+  constexpr int KSTEPS = KC / 16;
+  size_t smem = 2 * (2 * (size_t)KSTEPS * 4096 + 2 * (size_t)KSTEPS * nwmax * 32);
+  // at least 116 KB so that one CTA (and its 512 TMEM columns) fits per SM
+  if (smem < 118784) smem = 118784;
+  static int attr_bytes = -1;
+  if (attr_bytes < 0) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_contract_tc<BF16, KC>) != cudaSuccess) return MG_ERR_CUDA;
+    attr_bytes = 227 * 1024 - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(k_contract_tc<BF16, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             attr_bytes) != cudaSuccess)
+      return MG_ERR_CUDA;
+  }
+  if ((int)smem > attr_bytes) return MG_ERR_UNSUPPORTED;
+  k_contract_tc<BF16, KC><<<num_sms, TC_THREADS, smem, s>>>(g, w, spectra, cube, nwmax);
+  return MG_OK;
+}
+
+int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
+                           int num_sms, cudaStream_t s) {
+  const int nwmax = w.seg_width;  // a stage window never exceeds the padded band
+  if (nwmax > TC_TMEM_COLS) return MG_ERR_UNSUPPORTED;
+  const bool bf16 = g.form == MG_FORM_BF16X3;
+  int rc;
+  if (nwmax <= 256)
+    rc = bf16 ? launch_tc<true, 64>(g, w, spectra, cube, num_sms, s, nwmax)
+              : launch_tc<false, 64>(g, w, spectra, cube, num_sms, s, nwmax);
+  else
+    rc = bf16 ? launch_tc<true, 32>(g, w, spectra, cube, num_sms, s, nwmax)
+              : launch_tc<false, 32>(g, w, spectra, cube, num_sms, s, nwmax);
+  if (rc) return rc;
+  k_reduce_partials_tc<<<num_sms * 8, 256, 0, s>>>(g, w, cube);
+  return MG_OK;
+}
+
+}  // namespace mg

@@ -1,0 +1,169 @@
+"""Device-side insertion engine: owns the workspace and drives the C ABI.
+
+``InsertionEngine.insert`` takes particle arrays already on the GPU (torch
+tensors), runs ``mg_plan`` (footprint binning, sizes the workspace; one
+host synchronisation) and ``mg_insert`` (everything else, asynchronous) on
+the current CUDA stream, and returns the float32 cube and FP64 flux sums on
+the device.  PyTorch supplies device memory and streams only; all compute
+is in ``libmartini_gb300.so``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+
+@dataclass
+class DeviceParticles:
+    """Particle inputs in device memory (one entry per particle)."""
+
+    x: torch.Tensor                      # f64 pixel coordinate, axis 0
+    y: torch.Tensor                      # f64 pixel coordinate, axis 1
+    sm_range: torch.Tensor               # f64 footprint half-width, px
+    h_eff: torch.Tensor                  # f32 sm_length * rescale, px
+    kernel_index: torch.Tensor | None    # i8 kernel table index (-1 -> 0) or None
+    v: torch.Tensor | None = None        # f64 line-of-sight velocity, km/s
+    sigma: torch.Tensor | None = None    # f32 Gaussian width, km/s
+    amp: torch.Tensor | None = None      # f64 mHI / D^2 / 2.36e5
+    spectra: torch.Tensor | None = None  # f32 [n, nc] (table model)
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    @staticmethod
+    def from_host(device, x, y, sm_range, h_eff, kernel_index=None, v=None, sigma=None, amp=None,
+                  spectra=None) -> "DeviceParticles":
+        def put(a, dt):
+            if a is None:
+                return None
+            t = torch.from_numpy(np.ascontiguousarray(a, dtype=dt))
+            if device.type == "cuda":
+                t = t.pin_memory().to(device, non_blocking=True)
+            return t
+        return DeviceParticles(put(x, np.float64), put(y, np.float64), put(sm_range, np.float64),
+                               put(h_eff, np.float32), put(kernel_index, np.int8),
+                               put(v, np.float64), put(sigma, np.float32), put(amp, np.float64),
+                               put(spectra, np.float32))
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class InsertionEngine:
+    """Owns a reusable device workspace for repeated insertions."""
+
+    def __init__(self, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("martini_gb300 needs a CUDA GPU (no CPU fallback)")
+        self.lib = N.load()
+        self.device = torch.device(device) if device is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        self._ws = None
+        self._caps = (0, 0)
+        self.last_plan = None
+
+    # ---- problem description ------------------------------------------------
+    def problem(self, parts: DeviceParticles, kernels, spectral_model: int, sigma_const: float,
+                nx: int, ny: int, nc: int, padx: int, pady: int, edges: torch.Tensor,
+                cube: torch.Tensor, flux: torch.Tensor | None, form: int) -> N.Problem:
+        p = N.Problem()
+        p.n = parts.n
+        p.x, p.y, p.sm_range = _ptr(parts.x), _ptr(parts.y), _ptr(parts.sm_range)
+        p.h_eff, p.kernel_index = _ptr(parts.h_eff), _ptr(parts.kernel_index)
+        if not 1 <= len(kernels) <= N.MG_MAX_KERNELS:
+            raise ValueError("1 to 4 kernels")
+        p.n_kernels = len(kernels)
+        for k, (t, trunc) in enumerate(kernels):
+            p.kernels[k].type = int(t)
+            p.kernels[k].truncate = float(trunc)
+        p.spectral_model = int(spectral_model)
+        p.v, p.sigma, p.amp, p.spectra = (_ptr(parts.v), _ptr(parts.sigma), _ptr(parts.amp),
+                                          _ptr(parts.spectra))
+        p.sigma_const = float(sigma_const)
+        p.nx, p.ny, p.nc, p.padx, p.pady = int(nx), int(ny), int(nc), int(padx), int(pady)
+        p.edges = _ptr(edges)
+        p.cube = _ptr(cube)
+        p.flux = _ptr(flux)
+        p.form = int(form)
+        return p
+
+    def _workspace(self, nbytes: int) -> torch.Tensor:
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(max(nbytes, 1 << 16), dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def plan(self, prob: N.Problem, stream=None) -> N.PlanInfo:
+        """Bin the particles and size the workspace (synchronises the stream)."""
+        s = stream or torch.cuda.current_stream(self.device)
+        base = C.c_size_t()
+        N.check(self.lib.mg_workspace_size(C.byref(prob), 0, 0, C.byref(base)))
+        ws = self._workspace(base.value)
+        info = N.PlanInfo()
+        N.check(self.lib.mg_plan(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                 C.c_void_p(s.cuda_stream), C.byref(info)))
+        self._caps = (int(info.n_pairs), int(info.n_partial_items))
+        need = C.c_size_t()
+        N.check(self.lib.mg_workspace_size(C.byref(prob), self._caps[0], self._caps[1],
+                                           C.byref(need)))
+        self._workspace(need.value)
+        self.last_plan = info
+        return info
+
+    def run(self, prob: N.Problem, stream=None) -> None:
+        """Full insertion with the capacities of the last plan (asynchronous)."""
+        s = stream or torch.cuda.current_stream(self.device)
+        ws = self._ws
+        N.check(self.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                   self._caps[0], self._caps[1], C.c_void_p(s.cuda_stream)))
+
+    def run_stages(self, prob: N.Problem, stages: int, stream=None) -> None:
+        """Some stages of mg_insert (N.MG_STAGE_* bits), asynchronous."""
+        s = stream or torch.cuda.current_stream(self.device)
+        ws = self._ws
+        N.check(self.lib.mg_insert_stages(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                          self._caps[0], self._caps[1], int(stages),
+                                          C.c_void_p(s.cuda_stream)))
+
+    def check(self, stream=None) -> None:
+        s = stream or torch.cuda.current_stream(self.device)
+        N.check(self.lib.mg_check(C.c_void_p(self._ws.data_ptr()), C.c_void_p(s.cuda_stream)))
+
+    def insert(self, parts: DeviceParticles, kernels, spectral_model: int, sigma_const: float,
+               nx: int, ny: int, nc: int, edges: torch.Tensor, padx: int = 0, pady: int = 0,
+               form: int = N.MG_FORM_FP32, cube: torch.Tensor | None = None, flux: bool = True,
+               plan: bool = True, check: bool = True):
+        """Insert particles into a (nx, ny, nc) float32 cube (Jy/pix^2).
+
+        Returns (cube, flux) device tensors; flux[0] is the total flux in Jy
+        over the unpadded region and flux[1:] the per-channel sums.
+        """
+        if cube is None:
+            cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=self.device)
+        fl = torch.empty(nc + 1, dtype=torch.float64, device=self.device) if flux else None
+        prob = self.problem(parts, kernels, spectral_model, sigma_const, nx, ny, nc, padx, pady,
+                            edges, cube, fl, form)
+        if plan or self._ws is None:
+            self.plan(prob)
+        self.run(prob)
+        if check:
+            self.check()
+        return cube, fl
+
+    def spectra(self, parts: DeviceParticles, spectral_model: int, sigma_const: float, nc: int,
+                edges: torch.Tensor) -> torch.Tensor:
+        """Materialised spectra [n, nc] (Jy) of a GAUSSIAN/DIRAC model."""
+        out = torch.empty((parts.n, nc), dtype=torch.float32, device=self.device)
+        dummy = torch.empty(1, dtype=torch.float32, device=self.device)
+        prob = self.problem(parts, [(N.MG_KERNEL_DIRAC, 0.0)], spectral_model, sigma_const, 1, 1,
+                            nc, 0, 0, edges, dummy, None, N.MG_FORM_FP32)
+        N.check(self.lib.mg_spectra(C.byref(prob), C.c_void_p(out.data_ptr()),
+                                    C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
+        return out

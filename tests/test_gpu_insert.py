@@ -1,0 +1,249 @@
+"""GPU parity: the CUDA insertion against the reference's golden cubes and
+the FP64 oracle.  Tolerances: max |cube - ref| / peak(ref) <= 1e-5 and
+|flux - ref flux| / ref flux <= 1e-6 (FP32 form)."""
+
+import numpy as np
+import pytest
+import torch
+
+from tests.helpers import case_inputs, golden_cases, load_case, native_kernel_table
+from oracle import martini_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL_PEAK = 1e-5
+TOL_FLUX = 1e-6
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from martini_gb300.engine import InsertionEngine
+    return InsertionEngine("cuda:0")
+
+
+def run_gpu(engine, c, form=0, plan=True):
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    dev = engine.device
+    parts = DeviceParticles.from_host(dev, c["x"], c["y"], c["ranges"], c["h_eff"], c["kidx"],
+                                      v=c["v"], sigma=c["sigma"], amp=c["amp"])
+    model = N.MG_SPECTRUM_GAUSSIAN if c["spectral"] == "gaussian" else N.MG_SPECTRUM_DIRAC
+    edges = torch.from_numpy(np.ascontiguousarray(c["edges"], dtype=np.float64)).to(dev)
+    cube, flux = engine.insert(parts, native_kernel_table(c["kernels"]), model, 0.0, c["nx"],
+                               c["ny"], c["nc"], edges, padx=c["pad"], pady=c["pad"], form=form,
+                               plan=plan)
+    return cube.cpu().numpy().astype(np.float64), flux.cpu().numpy()
+
+
+def assert_close(got, ref, flux=None, pad=0, tol=TOL_PEAK):
+    peak = np.abs(ref).max()
+    err = np.abs(got - ref).max() / peak
+    assert err <= tol, f"max err / peak = {err:.3e}"
+    if flux is not None:
+        sl = (slice(pad, ref.shape[0] - pad), slice(pad, ref.shape[1] - pad))
+        tot = ref[sl].sum()
+        ferr = abs(flux[0] - tot) / tot
+        assert ferr <= TOL_FLUX, f"flux rel err = {ferr:.3e}"
+        np.testing.assert_allclose(flux[1:], ref[sl].sum(axis=(0, 1)), rtol=1e-5,
+                                   atol=1e-6 * np.abs(ref[sl].sum(axis=(0, 1))).max())
+
+
+FORMS = [0, 1, 2]  # MG_FORM_FP32, MG_FORM_BF16X3, MG_FORM_F16X3
+FORM_IDS = ["fp32", "bf16x3", "f16x3"]
+# the BF16 hi+lo split keeps ~16 mantissa bits: per term 3 * 2^-18 = 1.1e-5
+# relative in the worst case, so a voxel dominated by one particle can miss
+# 1e-5 of the peak; FP32 and the scaled FP16 split (3 * 2^-22) are held to it
+FORM_TOL = {0: 1e-5, 1: 2e-5, 2: 1e-5}
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_cube(engine, case, form):
+    d = load_case(case)
+    c = case_inputs(d)
+    assert len(c["x"]) == int(d["n_after"])
+    got, flux = run_gpu(engine, c, form=form)
+    assert_close(got, d["cube"], flux, c["pad"], tol=FORM_TOL[form])
+
+
+def test_martini_api_matches_oracle():
+    """Martini(...).insert_source_in_cube() end to end against the oracle."""
+    from martini_gb300 import DataCube, Martini, SPHSource
+    from martini_gb300.sph_kernels import WendlandC2Kernel
+    from martini_gb300.spectral_models import GaussianSpectrum
+    g = orc.disc_particles(4000, seed=11, h_med=0.6)
+    xyz, vxyz = orc.incline(g["xyz"], g["vxyz"], 50.0)
+    src = SPHSource(distance=3.0, T_g=g["T"], mHI_g=g["mHI"], xyz_g=xyz, vxyz_g=vxyz,
+                    hsm_g=g["hsm"])
+    dc = DataCube(n_px_x=48, n_px_y=40, n_channels=40, px_size=10.0, channel_width=4.0,
+                  spectral_centre=src.vsys)
+    m = Martini(source=src, datacube=dc, sph_kernel=WendlandC2Kernel(),
+                spectral_model=GaussianSpectrum(sigma="thermal"), quiet=True)
+    m.insert_source_in_cube()
+    k = m.sph_kernel
+    spectra = orc.init_spectra("gaussian", src.mHI_g, src.skycoords.distance,
+                               src.skycoords.radial_velocity, dc.velocity_channel_edges,
+                               orc.thermal_sigma_kms(src.T_g))
+    ref = orc.insert_scatter(48, 40, src.pixcoords[0], src.pixcoords[1], k.sm_ranges,
+                             orc.adaptive_tuple("WendlandC2Kernel"), k.kernel_indices,
+                             k.sm_lengths * k._rescale, spectra) / 100.0
+    assert dc._array_unit == "Jy/arcsec2"
+    assert_close(dc._array, ref)
+    assert m.inserted_flux_density == pytest.approx(ref.sum() * 100.0, rel=TOL_FLUX)
+
+
+def test_insert_accumulates_into_existing_array():
+    """_array += (martini/martini.py:338): prior contents are kept."""
+    from martini_gb300 import DataCube, Martini, SPHSource
+    from martini_gb300.sph_kernels import CubicSplineKernel
+    from martini_gb300.spectral_models import GaussianSpectrum
+    g = orc.disc_particles(500, seed=2)
+    src = SPHSource(distance=3.0, mHI_g=g["mHI"], xyz_g=g["xyz"], vxyz_g=g["vxyz"],
+                    hsm_g=g["hsm"])
+    dc = DataCube(n_px_x=16, n_px_y=16, n_channels=16, px_size=15.0, channel_width=4.0,
+                  spectral_centre=src.vsys)
+    m = Martini(source=src, datacube=dc, sph_kernel=CubicSplineKernel(),
+                spectral_model=GaussianSpectrum(), quiet=True)
+    m.insert_source_in_cube()
+    once = dc._array.copy()
+    m.insert_source_in_cube()
+    np.testing.assert_allclose(dc._array, 2 * once, rtol=1e-12)
+    m.reset()
+    assert dc._array.sum() == 0
+    m.insert_source_in_cube()
+    np.testing.assert_allclose(dc._array, once, rtol=1e-12)
+
+
+def test_spectra_materialised_match_oracle(engine):
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    sv = np.load("tests/golden/spectra_vectors.npz")
+    for tag in ("vrad", "incr", "freq"):
+        v, sig, mHI, dist = sv[f"v_{tag}"], sv[f"sigma_{tag}"], sv[f"mHI_{tag}"], sv[f"dist_{tag}"]
+        edges = sv[f"edges_{tag}"]
+        n = v.size
+        parts = DeviceParticles.from_host(engine.device, np.zeros(n), np.zeros(n), np.ones(n),
+                                          np.ones(n), None, v=v, sigma=sig,
+                                          amp=mHI / dist**2 / orc.MHI_TO_JY)
+        e = torch.from_numpy(edges).to(engine.device)
+        for model, key in ((N.MG_SPECTRUM_GAUSSIAN, "gaussian"), (N.MG_SPECTRUM_DIRAC, "dirac")):
+            got = engine.spectra(parts, model, 0.0, edges.size - 1, e).cpu().numpy()
+            ref = sv[f"{key}_{tag}"]
+            np.testing.assert_allclose(got, ref, rtol=0, atol=1e-6 * np.abs(ref).max())
+
+
+def test_empty_and_outside(engine):
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    edges = torch.from_numpy(orc.vrad_channel_edges(8, 4.0, 100.0)).to(engine.device)
+    for x in (np.zeros(0), np.array([-50.0, 80.0, np.nan])):
+        n = x.size
+        parts = DeviceParticles.from_host(engine.device, x, np.zeros(n), np.full(n, 2.0),
+                                          np.full(n, 1.5), None, v=np.full(n, 100.0),
+                                          sigma=np.full(n, 5.0), amp=np.ones(n))
+        cube, flux = engine.insert(parts, [(N.MG_KERNEL_WENDLAND_C2, 0.0)],
+                                   N.MG_SPECTRUM_GAUSSIAN, 0.0, 12, 10, 8, edges)
+        assert float(cube.abs().max()) == 0.0
+        assert float(flux[0]) == 0.0
+
+
+def test_nonmonotonic_edges_raise(engine):
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    e = orc.vrad_channel_edges(8, 4.0, 100.0)
+    e[4] = e[2]
+    parts = DeviceParticles.from_host(engine.device, np.array([3.0]), np.array([3.0]),
+                                      np.array([2.0]), np.array([1.5]), None,
+                                      v=np.array([100.0]), sigma=np.array([5.0]),
+                                      amp=np.array([1.0]))
+    with pytest.raises(ValueError, match="not monotonic"):
+        engine.insert(parts, [(N.MG_KERNEL_WENDLAND_C2, 0.0)], N.MG_SPECTRUM_GAUSSIAN, 0.0, 8, 8,
+                      8, torch.from_numpy(e).to(engine.device))
+
+
+def test_workspace_overflow_is_reported(engine):
+    """A workspace sized for fewer pairs than the data need: no write past it,
+    MG_ERR_WORKSPACE from mg_check."""
+    import ctypes as C
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    rng = np.random.default_rng(0)
+    n = 200
+    parts = DeviceParticles.from_host(engine.device, rng.uniform(0, 32, n), rng.uniform(0, 32, n),
+                                      np.full(n, 12.0), np.full(n, 7.0), None,
+                                      v=np.full(n, 100.0), sigma=np.full(n, 5.0), amp=np.ones(n))
+    edges = torch.from_numpy(orc.vrad_channel_edges(8, 4.0, 100.0)).to(engine.device)
+    cube = torch.empty((32, 32, 8), dtype=torch.float32, device=engine.device)
+    prob = engine.problem(parts, [(N.MG_KERNEL_WENDLAND_C2, 0.0)], N.MG_SPECTRUM_GAUSSIAN, 0.0,
+                          32, 32, 8, 0, 0, edges, cube, None, N.MG_FORM_FP32)
+    info = engine.plan(prob)
+    small = C.c_size_t()
+    N.check(engine.lib.mg_workspace_size(C.byref(prob), info.n_pairs // 2, 0, C.byref(small)))
+    ws = torch.zeros(small.value, dtype=torch.uint8, device=engine.device)
+    s = torch.cuda.current_stream().cuda_stream
+    N.check(engine.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                 info.n_pairs // 2, 0, C.c_void_p(s)))
+    assert engine.lib.mg_check(C.c_void_p(ws.data_ptr()), C.c_void_p(s)) == N.MG_ERR_WORKSPACE
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+def test_flux_conservation_medium(engine, form):
+    """A 20k-particle WendlandC2 disc on 128^2 x 64: full-cube parity."""
+    rng_seed = 21
+    g = orc.disc_particles(20000, seed=rng_seed, h_med=1.0)
+    xyz, vxyz = orc.incline(g["xyz"], g["vxyz"], 60.0)
+    ra, dec, v, d = orc.project_particles(xyz, vxyz, 3.0)
+    x, y = orc.tan_world2pix(ra, dec, 0.0, 0.0, 64.5, 64.5, -10 / 3600, 10 / 3600)
+    hpx = orc.sm_lengths_px(g["hsm"], d, 10.0)
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    kidx, size, resc = orc.select_kernels(kernels, hpx)
+    ranges = orc.sm_ranges(hpx, size)
+    edges = orc.vrad_channel_edges(64, 4.0, 210.0)
+    sig = orc.thermal_sigma_kms(g["T"])
+    vchan = 31.5 + (v - 210.0) / -4.0
+    keep = orc.prune_mask(x, y, vchan, ranges, g["mHI"], 128, 128, 64, sig, edges)
+    c = dict(x=x[keep], y=y[keep], ranges=ranges[keep], h_eff=(hpx * resc)[keep],
+             kidx=kidx[keep], v=v[keep], sigma=sig[keep],
+             amp=(g["mHI"] / d**2 / orc.MHI_TO_JY)[keep], kernels=kernels, spectral="gaussian",
+             edges=edges, nx=128, ny=128, nc=64, pad=0)
+    spectra = orc.init_spectra("gaussian", g["mHI"][keep], d[keep], v[keep], edges, sig[keep])
+    ref = orc.insert_scatter(128, 128, c["x"], c["y"], c["ranges"], kernels, c["kidx"],
+                             c["h_eff"], spectra)
+    got, flux = run_gpu(engine, c, form=form)
+    assert_close(got, ref, flux, tol=FORM_TOL[form])
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+def test_insertion_is_deterministic(engine, form):
+    """Stable sort + fixed split-K order: two runs give identical bits."""
+    d = load_case("cfg1_disc_cubic")
+    c = case_inputs(d)
+    a, fa = run_gpu(engine, c, form=form)
+    b, fb = run_gpu(engine, c, form=form, plan=False)
+    assert np.array_equal(a, b)
+    assert np.array_equal(fa, fb)
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+def test_split_k_large_tile_matches_oracle(engine, form):
+    """Thousands of particles on one tile: several K chunks per segment, the
+    split-K partial reduction, against the oracle."""
+    rng = np.random.default_rng(17)
+    n = 9000
+    x = rng.normal(6.0, 1.5, n)
+    y = rng.normal(9.0, 2.5, n)
+    h = 10 ** rng.uniform(0.2, 0.6, n)
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    kidx, size, resc = orc.select_kernels(kernels, h)
+    ranges = orc.sm_ranges(h, size)
+    edges = orc.vrad_channel_edges(96, 4.0, 300.0)
+    v = rng.uniform(150, 450, n)
+    sig = rng.uniform(4, 12, n)
+    mHI = 10 ** rng.uniform(4, 5, n)
+    c = dict(x=x, y=y, ranges=ranges, h_eff=h * resc, kidx=kidx, v=v, sigma=sig,
+             amp=mHI / 9.0 / orc.MHI_TO_JY, kernels=kernels, spectral="gaussian", edges=edges,
+             nx=20, ny=24, nc=96, pad=0)
+    spectra = orc.init_spectra("gaussian", mHI, np.full(n, 3.0), v, edges, sig)
+    ref = orc.insert_scatter(20, 24, x, y, ranges, kernels, kidx, h * resc, spectra)
+    got, flux = run_gpu(engine, c, form=form)
+    assert_close(got, ref, flux, tol=FORM_TOL[form])

@@ -1,0 +1,157 @@
+"""Host-side set-up of the drop-in API (projection, kernel selection,
+pruning, channel grid) against the oracle's restatement (CPU only)."""
+
+import numpy as np
+import pytest
+
+from martini_gb300 import DataCube, SPHSource
+from martini_gb300.martini import _BaseMartini
+from martini_gb300 import sph_kernels as K
+from martini_gb300 import spectral_models as S
+from oracle import martini_oracle as orc
+
+
+def disc_source(n=2000, seed=3, D=3.0, incl=60.0, **kw):
+    g = orc.disc_particles(n, seed=seed, **kw)
+    xyz, vxyz = orc.incline(g["xyz"], g["vxyz"], incl)
+    return g, xyz, vxyz, SPHSource(distance=D, T_g=g["T"], mHI_g=g["mHI"], xyz_g=xyz,
+                                    vxyz_g=vxyz, hsm_g=g["hsm"])
+
+
+class _NoGPU(_BaseMartini):
+    """_BaseMartini set-up only (no insertion)."""
+
+
+@pytest.mark.parametrize("ra,dec", [(0.0, 0.0), (30.0, -30.0), (200.0, 45.0)])
+def test_pixcoords_match_oracle(ra, dec):
+    g, xyz, vxyz, _ = disc_source()
+    src = SPHSource(distance=3.0, ra=ra, dec=dec, T_g=g["T"], mHI_g=g["mHI"], xyz_g=xyz,
+                    vxyz_g=vxyz, hsm_g=g["hsm"], vpeculiar=50.0)
+    dc = DataCube(n_px_x=64, n_px_y=48, n_channels=32, px_size=10.0, channel_width=4.0,
+                  spectral_centre=src.vsys, ra=ra, dec=dec)
+    src._init_skycoords()
+    src._init_pixcoords(dc)
+    ra_p, dec_p, v, d = orc.project_particles(xyz, vxyz, 3.0, ra, dec, 0.7, 50.0)
+    x, y = orc.tan_world2pix(ra_p, dec_p, ra, dec, 32.5, 24.5, -10 / 3600, 10 / 3600)
+    vchan = 15.5 + (v - src.vsys) / -4.0
+    np.testing.assert_allclose(src.pixcoords[0], x, atol=1e-9)
+    np.testing.assert_allclose(src.pixcoords[1], y, atol=1e-9)
+    np.testing.assert_allclose(src.pixcoords[2], vchan, atol=1e-9)
+    np.testing.assert_allclose(src.skycoords.radial_velocity, v, rtol=1e-13)
+
+
+def test_pixcoords_known_answer():
+    """tests/test_sources.py:335-380 of the reference."""
+    D = 1e-3 / np.deg2rad(1 / 3600.0)
+    yz = np.linspace(-2.5, 2.5, 6)
+    src = SPHSource(distance=D, h=0.0, T_g=np.ones(6) * 1e4, mHI_g=np.ones(6) * 1e4,
+                    xyz_g=np.vstack((np.zeros(6), yz, yz)).T,
+                    vxyz_g=np.vstack((np.linspace(-2.5, 2.5, 6), np.zeros(6), np.zeros(6))).T,
+                    hsm_g=np.ones(6))
+    dc = DataCube(n_px_x=6, n_px_y=6, n_channels=6, px_size=1.0, channel_width=1.0)
+    src._init_skycoords()
+    src._init_pixcoords(dc)
+    exp = np.vstack((np.arange(6)[::-1], np.arange(6), np.arange(6)[::-1]))
+    np.testing.assert_allclose(src.pixcoords, exp, atol=1e-4)
+
+
+def test_channel_edges():
+    dc = DataCube(n_px_x=4, n_px_y=4, n_channels=16, px_size=15.0, channel_width=4.0,
+                  spectral_centre=210.0)
+    np.testing.assert_allclose(dc.velocity_channel_edges, orc.vrad_channel_edges(16, 4.0, 210.0))
+    dcf = DataCube(n_px_x=4, n_px_y=4, n_channels=16, px_size=15.0, channel_width=20e3,
+                   spectral_centre=1.4194e9, freq_channels=True)
+    np.testing.assert_allclose(dcf.velocity_channel_edges,
+                               orc.freq_channel_edges(16, 20e3, 1.4194e9), rtol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["WendlandC2Kernel", "WendlandC6Kernel", "CubicSplineKernel",
+                                  "QuarticSplineKernel", "GaussianKernel"])
+def test_kernel_setup_matches_oracle(name):
+    g, xyz, vxyz, src = disc_source(h_med=0.3, h_dex=0.6)
+    dc = DataCube(n_px_x=64, n_px_y=64, n_channels=32, px_size=10.0, channel_width=4.0,
+                  spectral_centre=src.vsys)
+    k = getattr(K, name)()
+    src._init_skycoords()
+    src._init_pixcoords(dc)
+    k._init_sm_lengths(src, dc)
+    k._init_sm_ranges()
+    ra, dec, v, d = orc.project_particles(xyz, vxyz, 3.0)
+    hpx = orc.sm_lengths_px(g["hsm"], d, 10.0)
+    np.testing.assert_allclose(k.sm_lengths, hpx, rtol=1e-14)
+    idx, size, resc = orc.select_kernels(orc.adaptive_tuple(name), hpx)
+    np.testing.assert_array_equal(k.kernel_indices, idx)
+    np.testing.assert_array_equal(k.sm_ranges, orc.sm_ranges(hpx, size))
+    np.testing.assert_allclose(k._rescale, resc, rtol=1e-15)
+    assert set(np.unique(idx)) >= {0, 1, 2}
+
+
+def test_adaptive_known_answer():
+    src = SPHSource(distance=3.0, mHI_g=np.ones(4) * 1e4, xyz_g=np.ones((4, 3)) * 1e-3,
+                    vxyz_g=np.zeros((4, 3)), hsm_g=np.array([3.0, 1.0, 0.55, 0.1]))
+    px = np.rad2deg(np.arctan(1.0 / 3000.0)) * 3600  # 1 kpc pixels at 3 Mpc
+    dc = DataCube(n_px_x=10, n_px_y=10, n_channels=8, px_size=px, channel_width=4.0)
+    src._init_skycoords()
+    for cls in (K.WendlandC2Kernel, K.WendlandC6Kernel, K.CubicSplineKernel,
+                K.QuarticSplineKernel):
+        k = cls()
+        k._init_sm_lengths(src, dc)
+        assert list(k.kernel_indices) == [0, 0, 2, 1]
+    k = K.GaussianKernel(truncate=3.0)
+    k._init_sm_lengths(src, dc)
+    assert list(k.kernel_indices) == [0, 2, 2, 1]
+
+
+@pytest.mark.parametrize("spectral", ["gaussian", "dirac", "thermal"])
+def test_pruning_matches_oracle(spectral):
+    g, xyz, vxyz, src = disc_source(n=3000)
+    dc = DataCube(n_px_x=32, n_px_y=32, n_channels=16, px_size=10.0, channel_width=4.0,
+                  spectral_centre=src.vsys)
+    sm = {"gaussian": S.GaussianSpectrum(7.0), "dirac": S.DiracDeltaSpectrum(),
+          "thermal": S.GaussianSpectrum("thermal")}[spectral]
+    m = _NoGPU(source=src, datacube=dc, sph_kernel=K.CubicSplineKernel(), spectral_model=sm,
+               quiet=True)
+    ra, dec, v, d = orc.project_particles(xyz, vxyz, 3.0)
+    x, y = orc.tan_world2pix(ra, dec, 0.0, 0.0, 16.5, 16.5, -10 / 3600, 10 / 3600)
+    vchan = 7.5 + (v - 210.0) / -4.0
+    hpx = orc.sm_lengths_px(g["hsm"], d, 10.0)
+    _, size, _ = orc.select_kernels(orc.adaptive_tuple("CubicSplineKernel"), hpx)
+    hw = {"gaussian": 7.0, "dirac": 0.0, "thermal": orc.thermal_sigma_kms(g["T"])}[spectral]
+    keep = orc.prune_mask(x, y, vchan, orc.sm_ranges(hpx, size), g["mHI"], 32, 32, 16, hw,
+                          dc.velocity_channel_edges)
+    assert m.source.npart == keep.sum()
+    np.testing.assert_allclose(m.source.pixcoords[0], x[keep], atol=1e-9)
+
+
+def test_prune_all_raises():
+    src = SPHSource(distance=3.0, mHI_g=np.zeros(2), xyz_g=np.zeros((2, 3)),
+                    vxyz_g=np.zeros((2, 3)), hsm_g=np.ones(2))
+    dc = DataCube(n_px_x=8, n_px_y=8, n_channels=8, px_size=10.0, channel_width=4.0,
+                  spectral_centre=src.vsys)
+    with pytest.raises(RuntimeError, match="No non-zero mHI source particles"):
+        _NoGPU(source=src, datacube=dc, sph_kernel=K.CubicSplineKernel(),
+               spectral_model=S.GaussianSpectrum(), quiet=True)
+
+
+def test_validation_raises_like_reference():
+    src = SPHSource(distance=3.0, mHI_g=np.ones(1) * 1e4, xyz_g=np.ones((1, 3)) * 1e-3,
+                    vxyz_g=np.zeros((1, 3)), hsm_g=np.ones(1) * 0.2)
+    dc = DataCube(n_px_x=16, n_px_y=16, n_channels=16, px_size=15.0, channel_width=4.0,
+                  spectral_centre=src.vsys)
+    m = _NoGPU(source=src, datacube=dc, sph_kernel=K._WendlandC2Kernel(),
+               spectral_model=S.GaussianSpectrum(), quiet=True)
+    with pytest.raises(RuntimeError, match="use this with care"):
+        m.sph_kernel._confirm_validation(quiet=True)
+    m.sph_kernel._confirm_validation(noraise=True, quiet=True)
+
+
+def test_thermal_width_known_answer():
+    src = SPHSource(distance=3.0, T_g=np.array([1e4]), mHI_g=np.ones(1), xyz_g=np.zeros((1, 3)),
+                    vxyz_g=np.zeros((1, 3)), hsm_g=np.ones(1))
+    assert S.GaussianSpectrum("thermal").half_width(src)[0] == pytest.approx(9.0853727258,
+                                                                              rel=1e-10)
+
+
+def test_gaussian_truncation_below_two_raises():
+    with pytest.raises(RuntimeError, match="truncation <2sigma"):
+        K._GaussianKernel(truncate=1.0)
