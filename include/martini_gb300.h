@@ -181,6 +181,25 @@ int mg_flux(const float* cube, int32_t nx, int32_t ny, int32_t nc, int32_t padx,
             int32_t pady, double* flux, void* workspace, size_t workspace_bytes,
             void* stream);
 
+/*
+ * Size of the scratch array built into the library for mg_insert_noalloc
+ * (held on every GPU that loads the library until the process exits).
+ */
+#define MG_NOALLOC_SCRATCH_BYTES ((size_t)128 << 20)
+
+/*
+ * mg_insert without a caller workspace.  No counterpart in the reference:
+ * it exists for callers that cannot allocate GPU memory (code inside a
+ * framework or memory pool that owns every device allocation, or paths where
+ * an allocation is not allowed).  The scratch is a file-scope device array of
+ * MG_NOALLOC_SCRATCH_BYTES; problems whose binning needs more are rejected
+ * with MG_ERR_WORKSPACE and a message.  The first call on a device looks up
+ * the array's device address (make it before any stream capture).  Calls
+ * share the array: calls that overlap on the GPU race.  Synchronises the
+ * stream (it checks the status word); allocates nothing.
+ */
+int mg_insert_noalloc(const mg_problem* p, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,7 +40,9 @@ MG_MAX_KERNELS = 4
 
 # every symbol include/martini_gb300.h declares
 EXPORTS = ("mg_version", "mg_last_error", "mg_workspace_size", "mg_plan", "mg_insert",
-           "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux")
+           "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux", "mg_insert_noalloc")
+
+MG_NOALLOC_SCRATCH_BYTES = 128 << 20
 
 MG_STAGE_BIN = 1
 MG_STAGE_CONTRACT = 2
@@ -105,11 +107,12 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.mg_insert_stages.argtypes = [P(Problem), C.c_void_p, C.c_size_t, C.c_int64, C.c_int64,
                                      C.c_int32, C.c_void_p]
     lib.mg_check.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mg_insert_noalloc.argtypes = [P(Problem), C.c_void_p]
     lib.mg_spectra.argtypes = [P(Problem), C.c_void_p, C.c_void_p]
     lib.mg_flux.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                             C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
     for f in ("mg_workspace_size", "mg_plan", "mg_insert", "mg_insert_stages", "mg_check",
-              "mg_spectra", "mg_flux"):
+              "mg_spectra", "mg_flux", "mg_insert_noalloc"):
         getattr(lib, f).restype = C.c_int
     _lib = lib
     return lib

@@ -8,6 +8,10 @@
 
 using namespace mg;
 
+namespace mg {
+void set_last_error(const std::string& msg);
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -236,6 +240,8 @@ int workspace_view(const mg_problem* p, const Geo& g, void* ws, size_t bytes,
 }
 
 }  // namespace
+
+void mg::set_last_error(const std::string& msg) { g_err = msg; }
 
 extern "C" {
 
