@@ -136,8 +136,9 @@ __global__ void k_prep(PrepArgs a, Geo g, Ws w) {
         if (g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
           double s = a.sigma ? (double)a.sigma[p] : (double)g.sigma_const;
           rec.inv_s = (float)(1.0 / (1.4142135623730951 * s));
-          // |u| <= 6: beyond, erf differences are below 2e-17
-          double half = 6.0 * 1.4142135623730951 * s;
+          // |u| <= 4.5: beyond it each wing holds erfc(4.5) / 2 = 1e-10 of
+          // the line's flux
+          double half = 4.5 * 1.4142135623730951 * s;
           channel_range(a.edges, g.nc, dec, v - half, v + half, rec.clo, rec.chi);
         } else {
           channel_range(a.edges, g.nc, dec, v, v, rec.clo, rec.chi);

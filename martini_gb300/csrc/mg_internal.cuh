@@ -169,11 +169,12 @@ constexpr float kPi = 3.14159265358979323846f;
 __device__ __forceinline__ float kt_eval(int kt, float s) {
   const KTableInfo& inf = kt_info[kt];
   if (!(s < inf.smax)) return 0.f;
-  const float R = sqrtf(s);
+  const float R = s > 0.f ? s * rsqrtf(s) : 0.f;
   int r = 0;
   if (inf.nreg == 3) r = (s > 1.f) ? 2 : (R >= inf.split_r ? 1 : 0);
   const KRegion g = inf.reg[r];
-  const float v = g.var ? sqrtf(fmaxf(1.f - s, 0.f)) : R;
+  const float a2 = fmaxf(1.f - s, 0.f);
+  const float v = g.var ? (a2 > 0.f ? a2 * rsqrtf(a2) : 0.f) : R;
   const float u = (v - g.lo) * g.cells_per_unit;
   int c = (int)u;
   c = c < 0 ? 0 : (c >= g.ncell ? g.ncell - 1 : c);

@@ -37,6 +37,7 @@ constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
 // round-to-nearest FP32 adds, which bounds that drift to ~TC_DRAIN * 3 * KC/16
 // MMAs per partial sum.
 constexpr int TC_DRAIN = 2;
+constexpr int KT_SMEM_CELLS = 576;  // largest radial table (cubic spline)
 constexpr int TC_MASTER_COL = 256;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -241,6 +242,212 @@ __device__ __forceinline__ PRec empty_rec() {
   return z;
 }
 
+// Radial-kernel profile f(s), s = R^2, from the cell table in shared memory
+// (same cells and coefficients as kt_eval), written without branches so
+// that the four pixels of a lane evaluate in parallel.  Returns 0 outside
+// the support.
+template <bool CUBIC>
+__device__ __forceinline__ float kt_eval_smem(const KTableInfo& inf, const float4* __restrict__ tab,
+                                              float s) {
+  const float R = s * rsqrtf(fmaxf(s, 1e-30f));
+  int r = 0;
+  if (CUBIC) r = (s > 1.f) ? 2 : (R >= inf.split_r ? 1 : 0);
+  const KRegion g = CUBIC ? inf.reg[r] : inf.reg[0];
+  const float a2 = fmaxf(1.f - s, 0.f);
+  const float v = (CUBIC && g.var) ? a2 * rsqrtf(fmaxf(a2, 1e-30f)) : R;
+  const float u = (v - g.lo) * g.cells_per_unit;
+  const int c = min(max(__float2int_rz(u), 0), g.ncell - 1);
+  const float t = u - (float)c;
+  const float4 lo = tab[2 * (g.first + c)];
+  const float4 hi = tab[2 * (g.first + c) + 1];
+  // Estrin: (c0 + c1 t) + t^2 (c2 + c3 t) + t^4 ((c4 + c5 t) + t^2 (c6 + c7 t))
+  const float t2 = t * t;
+  const float t4 = t2 * t2;
+  const float p01 = fmaf(lo.y, t, lo.x), p23 = fmaf(lo.w, t, lo.z);
+  const float p45 = fmaf(hi.y, t, hi.x), p67 = fmaf(hi.w, t, hi.z);
+  const float f = fmaf(t4, fmaf(t2, p67, p45), fmaf(t2, p23, p01));
+  return s < inf.smax ? f : 0.f;
+}
+
+// 16-bit hi/lo halves of two values packed as (first | second << 16).
+template <bool BF16>
+__device__ __forceinline__ void split_pair(float a, float b, unsigned& hi, unsigned& lo) {
+  unsigned short ah, al, bh, bl;
+  split2<BF16>(a, ah, al);
+  split2<BF16>(b, bh, bl);
+  hi = (unsigned)ah | ((unsigned)bh << 16);
+  lo = (unsigned)al | ((unsigned)bl << 16);
+}
+
+// W of one particle at the four pixels of a lane: rows ib + 2 k, column j.
+__device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec* ks,
+                                         const float4* ktab, int ktab_type, int ib, int j,
+                                         float sw, float (&w)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) w[k] = 0.f;
+  if (!valid || j < r.jlo || j > r.jhi) return;
+  const KSpec kk = ks[r.kslot];
+  const float dy = (float)(r.yi - j) + r.yf;
+  float dx[4];
+  bool in[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = ib + 2 * k;
+    in[k] = i >= r.ilo && i <= r.ihi;
+    dx[k] = (float)(r.xi - i) + r.xf;
+  }
+  if (kk.type == MG_KERNEL_DIRAC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) w[k] = in[k] ? sw : 0.f;
+  } else if (kk.type == MG_KERNEL_GAUSSIAN) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      w[k] = in[k] ? w_gaussian(dx[k], dy, r.h, kk.truncate, kk.gnorm) * sw : 0.f;
+  } else {
+    const KTableInfo& inf = kt_info[kk.type];
+    const float fac = (kk.type == MG_KERNEL_CUBIC_SPLINE ? 4.f : 1.f) * r.inv_h2;
+    const float scale = inf.scale * r.inv_h2 * sw;
+    const float dy2 = dy * dy;
+    const float4* tab = kk.type == ktab_type
+                            ? ktab
+                            : reinterpret_cast<const float4*>(kt_coef);
+    if (kk.type == MG_KERNEL_CUBIC_SPLINE) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float f = kt_eval_smem<true>(inf, tab, fmaf(dx[k], dx[k], dy2) * fac);
+        w[k] = in[k] ? f * scale : 0.f;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float f = kt_eval_smem<false>(inf, tab, fmaf(dx[k], dx[k], dy2) * fac);
+        w[k] = in[k] ? f * scale : 0.f;
+      }
+    }
+  }
+}
+
+// A = W for particles (q, q + 1): lane l covers pixels l + 32 k, k = 0..3,
+// which share the column j = j0 + (l & 15).
+template <bool BF16>
+__device__ __forceinline__ void produce_w_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
+                                               const KSpec* ks, const float4* ktab,
+                                               int ktab_type, int q, int i0, int j0, int lane,
+                                               float sw, unsigned char* a_hi,
+                                               unsigned char* a_lo) {
+  const int j = j0 + (lane & 15);
+  const int ib = i0 + (lane >> 4);
+  float w0[4], w1[4];
+  weights4(r0, v0, ks, ktab, ktab_type, ib, j, sw, w0);
+  weights4(r1, v1, ks, ktab, ktab_type, ib, j, sw, w1);
+  // element (pixel p, particle q): K step q / 16, K core q / 8 % 2, (q % 8) * 2
+  const unsigned qoff = (unsigned)(q >> 4) * 4096u + (unsigned)((q >> 3) & 1) * 128u +
+                        (unsigned)(q & 7) * 2u;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int p = lane + 32 * k;
+    const unsigned off = qoff + (unsigned)(p >> 3) * 256u + (unsigned)(p & 7) * 16u;
+    unsigned hi, lo;
+    split_pair<BF16>(w0[k], w1[k], hi, lo);
+    *reinterpret_cast<unsigned*>(a_hi + off) = hi;
+    *reinterpret_cast<unsigned*>(a_lo + off) = lo;
+  }
+}
+
+// erfc(z) for z >= 0 by the Chebyshev-fitted form of Press, Teukolsky,
+// Vetterling & Flannery, Numerical Recipes (2nd ed., section 6.2, "erfcc"):
+// erfc(z) = t exp(-z^2 + P(t)), t = 1 / (1 + z / 2), fractional error below
+// 1.2e-7 for all z >= 0.  Cheaper than the library erfcf on the producer
+// path; the FP32 contraction form keeps erff/erfcf.
+__device__ __forceinline__ float erfc_nr(float z) {
+  const float t = __frcp_rn(fmaf(0.5f, z, 1.f));
+  float p = 0.17087277f;
+  p = fmaf(p, t, -0.82215223f);
+  p = fmaf(p, t, 1.48851587f);
+  p = fmaf(p, t, -1.13520398f);
+  p = fmaf(p, t, 0.27886807f);
+  p = fmaf(p, t, -0.18628806f);
+  p = fmaf(p, t, 0.09678418f);
+  p = fmaf(p, t, 0.37409196f);
+  p = fmaf(p, t, 1.00002368f);
+  p = fmaf(p, t, -1.26551223f);
+  return t * __expf(fmaf(-z, z, p));
+}
+
+// erfc(|u|) and sign of u at channel edge ge for a Gaussian line.
+__device__ __forceinline__ void edge_term(const PRec& r, int ge, const float* ehi,
+                                          const float* elo, float& cval, bool& pos) {
+  const float u = ((ehi[ge] - r.vhi) + (elo[ge] - r.vlo)) * r.inv_s;
+  pos = u >= 0.f;
+  cval = erfc_nr(fabsf(u));
+}
+
+// 0.5 [erf(b) - erf(a)] (a < b) from erfc(|a|), erfc(|b|) and the signs.
+__device__ __forceinline__ float half_diff_from_c(float ca, bool pa, float cb, bool pb) {
+  const float both = 0.5f * (pa ? ca - cb : cb - ca);
+  return (pa || !pb) ? both : 1.f - 0.5f * (ca + cb);
+}
+
+// B = S for particles (q, q + 1) over the window channels.  A Gaussian line
+// needs erfc at every window edge once: in step m lane l evaluates edge
+// 31 m + l and channel 31 m + l (l < 31) takes its upper index edge from
+// lane l + 1, so each step covers 31 channels with no repeated evaluation.
+template <bool BF16>
+__device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
+                                               int q, int w0, int nw, int nc, int dec, int model,
+                                               const float* ehi, const float* elo,
+                                               const float* inv_w, const float* spectra,
+                                               int pid0, int pid1, int lane, float ss,
+                                               unsigned char* b_hi, unsigned char* b_lo) {
+  const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
+                        (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
+  const bool gauss = model == MG_SPECTRUM_GAUSSIAN;
+  const int step = gauss ? 31 : 32;
+  for (int base = 0; base < nw; base += step) {  // warp-uniform
+    const int n = base + lane;
+    const int c = w0 + n;
+    float s0 = 0.f, s1 = 0.f;
+    if (gauss) {
+      float ca0 = 0.f, ca1 = 0.f;
+      bool pa0 = true, pa1 = true;
+      if (n <= nw && c <= nc) {
+        if (v0) edge_term(r0, c, ehi, elo, ca0, pa0);
+        if (v1) edge_term(r1, c, ehi, elo, ca1, pa1);
+      }
+      const float cb0 = __shfl_down_sync(0xffffffffu, ca0, 1);
+      const float cb1 = __shfl_down_sync(0xffffffffu, ca1, 1);
+      const bool pb0 = __shfl_down_sync(0xffffffffu, (int)pa0, 1) != 0;
+      const bool pb1 = __shfl_down_sync(0xffffffffu, (int)pa1, 1) != 0;
+      if (lane < 31 && n < nw && c < nc) {
+        const float iw = inv_w[c] * ss;
+        // edge c is the channel's lower edge for increasing edges, the upper
+        // one for decreasing edges
+        const float phi0 = dec ? half_diff_from_c(cb0, pb0, ca0, pa0)
+                               : half_diff_from_c(ca0, pa0, cb0, pb0);
+        const float phi1 = dec ? half_diff_from_c(cb1, pb1, ca1, pa1)
+                               : half_diff_from_c(ca1, pa1, cb1, pb1);
+        s0 = (v0 && c >= r0.clo && c <= r0.chi) ? r0.amp * iw * phi0 : 0.f;
+        s1 = (v1 && c >= r1.clo && c <= r1.chi) ? r1.amp * iw * phi1 : 0.f;
+      }
+    } else if (n < nw && c < nc) {
+      if (model == MG_SPECTRUM_DIRAC) {
+        if (v0 && c >= r0.clo && c <= r0.chi) s0 = r0.amp * inv_w[c] * ss;
+        if (v1 && c >= r1.clo && c <= r1.chi) s1 = r1.amp * inv_w[c] * ss;
+      } else {
+        if (v0 && c >= r0.clo && c <= r0.chi) s0 = spectra[(long long)pid0 * nc + c] * ss;
+        if (v1 && c >= r1.clo && c <= r1.chi) s1 = spectra[(long long)pid1 * nc + c] * ss;
+      }
+    }
+    if (n < nw && (!gauss || lane < 31)) {
+      const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
+      unsigned hi, lo;
+      split_pair<BF16>(s0, s1, hi, lo);
+      *reinterpret_cast<unsigned*>(b_hi + off) = hi;
+      *reinterpret_cast<unsigned*>(b_lo + off) = lo;
+    }
+  }
+}
+
 template <bool BF16, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict__ cube,
@@ -251,6 +458,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   __shared__ PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
+  __shared__ float4 s_ktab[2 * KT_SMEM_CELLS];
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
@@ -280,6 +488,21 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   const unsigned sbase = smem_u32(smem);
 
   if (tid < MG_MAX_KERNELS) s_ks[tid] = g.ks[tid];
+  // the table of the launch's radial kernel (at most one per kernel tuple)
+  int ktab_type = -1;
+  for (int k = 0; k < g.n_kernels; ++k)
+    if (g.ks[k].type <= MG_KERNEL_QUARTIC_SPLINE) ktab_type = g.ks[k].type;
+  if (ktab_type >= 0) {
+    const KTableInfo& inf = kt_info[ktab_type];
+    int ncell = 0;
+    for (int r = 0; r < inf.nreg; ++r) ncell += inf.reg[r].ncell;
+    if (ncell <= KT_SMEM_CELLS) {
+      const float4* src = reinterpret_cast<const float4*>(kt_coef) + 2 * inf.reg[0].first;
+      for (int e = tid; e < 2 * ncell; e += TC_THREADS) s_ktab[e] = src[e];
+    } else {
+      ktab_type = -1;
+    }
+  }
   if (tid == 0) {
     mbar_init(smem_u32(&bars[0]), 1);
     mbar_init(smem_u32(&bars[1]), 1);
@@ -405,35 +628,20 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
       unsigned char* const sa_lo = sa_hi + a_bytes;
       unsigned char* const sb_hi = sa_lo + a_bytes;
       unsigned char* const sb_lo = sb_hi + b_bytes;
-      // ---- A = W: task (pixel p, particle group q8): 8 values, 16 bytes
-      for (int task = tid; task < TILE_PX * GROUPS; task += TC_THREADS) {
-        const int p = task & (TILE_PX - 1);
-        const int q8 = task >> 7;
-        const int i = i0 + p / TILE_J, j = j0 + p % TILE_J;
-        float v[8];
+      // ---- A = W and B = S, particle-major: warp w owns particles
+      // w * PPW .. w * PPW + PPW - 1, taken in pairs
+      constexpr int PPW = KC / (TC_THREADS / 32);
 #pragma unroll
-        for (int e = 0; e < 8; ++e) v[e] = pixel_weight(recs[buf][q8 * 8 + e], s_ks, i, j) * sw;
-        const unsigned off =
-            (q8 >> 1) * 4096u + (unsigned)(p >> 3) * 256u + (q8 & 1) * 128u + (p & 7) * 16u;
-        store8<BF16>(sa_hi, sa_lo, off, v);
-      }
-      // ---- B = S: task (channel n of the window, particle group q8)
-      for (int task = tid; task < nw * GROUPS; task += TC_THREADS) {
-        const int n = task % nw;
-        const int q8 = task / nw;
-        const int c = w0 + n;
-        float v[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const int q = q8 * 8 + e;
-          v[e] = (c < g.nc && q < kn)
-                     ? tc_spectrum(recs[buf][q], g.spectral_model, c, dec, w.ehi, w.elo,
-                                   w.inv_w, spectra, s_pid[buf][q], g.nc) * ss
-                     : 0.f;
-        }
-        const unsigned off = (q8 >> 1) * ((unsigned)nw * 32u) + (unsigned)(n >> 3) * 256u +
-                             (q8 & 1) * 128u + (n & 7) * 16u;
-        store8<BF16>(sb_hi, sb_lo, off, v);
+      for (int pp = 0; pp < PPW; pp += 2) {
+        const int q = warp * PPW + pp;
+        const PRec r0 = recs[buf][q];
+        const PRec r1 = recs[buf][q + 1];
+        const bool v0 = q < kn, v1 = q + 1 < kn;
+        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - 2 * (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
+                             ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
+        produce_s_pair<BF16>(r0, r1, v0, v1, q, w0, nw, g.nc, dec, g.spectral_model, w.ehi,
+                             w.elo, w.inv_w, spectra, s_pid[buf][q], s_pid[buf][q + 1], lane,
+                             ss, sb_hi, sb_lo);
       }
       if (has_next && tid < KC) {
         recs[buf ^ 1][tid] = nrec;
