@@ -76,11 +76,35 @@ __device__ __forceinline__ void channel_range(const double* e, int nc, int dec, 
 
 
 // One thread per particle: exact footprint, Dirac pixel, spectral support,
-// packed record; tile histogram and per-tile channel window by atomics.
-__global__ void k_prep(PrepArgs a, Geo g, Ws w) {
+// packed record.  The tile histogram is kept in shared memory when the tile
+// count fits (PREP_SMEM_TILES) and flushed once per block; the per-tile
+// channel windows (needed only when a tile has several channel blocks) and
+// the header maxima are reduced per block before their global atomics, so
+// no address sees one atomic per particle.
+constexpr int PREP_THREADS = 256;
+constexpr int PREP_SMEM_TILES = 12288;
+
+__global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) {
+  extern __shared__ int s_count[];  // [ntiles] when the histogram is in shared memory
+  __shared__ int s_wmax;
+  __shared__ unsigned s_wb, s_sb;
+  const bool smem_hist = g.ntiles <= PREP_SMEM_TILES;
+  const bool windows = w.ncb_seg > 1;
+  if (smem_hist)
+    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x) s_count[t] = 0;
+  if (threadIdx.x == 0) {
+    s_wmax = 0;
+    s_wb = s_sb = 0u;
+  }
+  __syncthreads();
   const int dec = w.hdr->edges_dec;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.n;
-       p += (long long)gridDim.x * blockDim.x) {
+  int my_wmax = 0;
+  unsigned my_wb = 0u, my_sb = 0u;
+  // every thread of a block runs the same number of iterations
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < a.n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long p = base + threadIdx.x;
+    if (p >= a.n) continue;
     PRec rec;
     rec.ilo = 0; rec.ihi = -1; rec.jlo = 0; rec.jhi = -1;
     rec.clo = 1; rec.chi = 0;
@@ -162,27 +186,49 @@ __global__ void k_prep(PrepArgs a, Geo g, Ws w) {
       for (int tx = tx0; tx <= tx1; ++tx)
         for (int ty = ty0; ty <= ty1; ++ty) {
           int t = tx * g.nty + ty;
-          atomicAdd(&w.tile_count[t], 1);
-          atomicMin(&w.tile_wlo[t], rec.clo);
-          atomicMax(&w.tile_whi[t], rec.chi);
+          if (smem_hist) atomicAdd(&s_count[t], 1);
+          else atomicAdd(&w.tile_count[t], 1);
+          if (windows) {
+            atomicMin(&w.tile_wlo[t], rec.clo);
+            atomicMax(&w.tile_whi[t], rec.chi);
+          }
         }
-      atomicMax(&w.hdr->wmax, rec.chi - rec.clo);
+      my_wmax = max(my_wmax, rec.chi - rec.clo);
       if (g.form == MG_FORM_F16X3) {
         // magnitude bounds for the scaled FP16 split (non-negative floats
         // order like their bit patterns)
         const KSpec k = g.ks[ks];
         float wb = weight_bound(k.type, rec.inv_h2, k.gnorm);
-        atomicMax(&w.hdr->wbound_bits, __float_as_uint(wb));
+        my_wb = max(my_wb, __float_as_uint(wb));
         float sb = rec.amp;
         if (g.spectral_model == MG_SPECTRUM_TABLE) {
           sb = 0.f;
           for (int c = 0; c < g.nc; ++c) sb = fmaxf(sb, fabsf(a.spectra[p * g.nc + c]));
         }
-        atomicMax(&w.hdr->sbound_bits, __float_as_uint(sb));
+        my_sb = max(my_sb, __float_as_uint(sb));
       }
     }
     w.npairs[p] = np;
   }
+  my_wmax = __reduce_max_sync(0xffffffffu, my_wmax);
+  my_wb = __reduce_max_sync(0xffffffffu, my_wb);
+  my_sb = __reduce_max_sync(0xffffffffu, my_sb);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&s_wmax, my_wmax);
+    atomicMax(&s_wb, my_wb);
+    atomicMax(&s_sb, my_sb);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicMax(&w.hdr->wmax, s_wmax);
+    if (g.form == MG_FORM_F16X3) {
+      atomicMax(&w.hdr->wbound_bits, s_wb);
+      atomicMax(&w.hdr->sbound_bits, s_sb);
+    }
+  }
+  if (smem_hist)
+    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
+      if (s_count[t]) atomicAdd(&w.tile_count[t], s_count[t]);
 }
 
 __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_partial) {
@@ -357,7 +403,16 @@ void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cuda
                  long long cap_pairs, long long cap_partial) {
   k_tile_init<<<(g.ntiles + 255) / 256, 256, 0, s>>>(g, w, cap_pairs, cap_partial);
   k_edges<<<(g.nc + 256) / 256, 256, 0, s>>>(a.edges, g.nc, w);
-  if (a.n > 0) k_prep<<<grid_for(a.n, num_sms), 256, 0, s>>>(a, g, w);
+  if (a.n > 0) {
+    // with the histogram in shared memory every block flushes up to ntiles
+    // counts: fewer, longer-lived blocks
+    const bool smem_hist = g.ntiles <= PREP_SMEM_TILES;
+    const size_t hist_bytes = smem_hist ? sizeof(int) * (size_t)g.ntiles : 0;
+    unsigned blocks = grid_for(a.n, num_sms);
+    const unsigned per_sm = hist_bytes <= 16384 ? 8u : 4u;
+    if (smem_hist && blocks > per_sm * (unsigned)num_sms) blocks = per_sm * (unsigned)num_sms;
+    k_prep<<<blocks, PREP_THREADS, hist_bytes, s>>>(a, g, w);
+  }
   launch_scan(w.npairs, a.n, w.pair_off, w.scan_sums, nullptr, s);
   k_plan_tiles<<<1, 1024, 0, s>>>(g, w);
 }

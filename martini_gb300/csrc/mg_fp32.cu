@@ -161,26 +161,62 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
   }
 }
 
-// Split-K reduction: one CTA per segment with more than one K chunk; sums
-// the chunks in order (deterministic) and writes the cube block.
-__global__ void k_reduce_partials(Geo g, Ws w, float* __restrict__ cube) {
+// Split-K reduction, shared by every form: a segment with nk > 1 work items
+// left nk partial rows of TILE_PX x seg_width floats (pixel-major).  One
+// block per (segment, chunk of RED_CHUNK floats): each thread sums four
+// channels of one pixel over the rows in ascending row order, so the result
+// does not depend on scheduling, with RED_ROWS float4 loads in flight.
+constexpr int RED_THREADS = 256;
+constexpr int RED_CHUNK = RED_THREADS * 4;
+constexpr int RED_ROWS = 8;
+
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_partials(Geo g, Ws w,
+                                                                 float* __restrict__ cube) {
   if (w.hdr->status) return;
-  for (int sg = blockIdx.x; sg < w.nseg; sg += gridDim.x) {
+  const int width = w.seg_width;       // a multiple of 16 channels
+  const int per_row = TILE_PX * width;
+  const int nchunk = (per_row + RED_CHUNK - 1) / RED_CHUNK;
+  const long long units = (long long)w.nseg * nchunk;
+  for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+    const int sg = (int)(u / nchunk);
     const int nk = w.seg_part[sg];
     if (nk == 0) continue;
+    const int e = (int)(u - (long long)sg * nchunk) * RED_CHUNK + threadIdx.x * 4;
+    if (e >= per_row) continue;
+    const float4* src =
+        reinterpret_cast<const float4*>(w.partial + w.part_off[sg] * (long long)per_row + e);
+    const long long row4 = per_row / 4;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k0 = 0; k0 < nk; k0 += RED_ROWS) {
+      float4 v[RED_ROWS];
+#pragma unroll
+      for (int q = 0; q < RED_ROWS; ++q)
+        if (k0 + q < nk) v[q] = __ldcs(src + (long long)(k0 + q) * row4);
+#pragma unroll
+      for (int q = 0; q < RED_ROWS; ++q)
+        if (k0 + q < nk) {
+          acc.x += v[q].x;
+          acc.y += v[q].y;
+          acc.z += v[q].z;
+          acc.w += v[q].w;
+        }
+    }
     const int t = sg / w.ncb_seg;
     const int cb = sg - t * w.ncb_seg;
-    const int tx = t / g.nty, ty = t - (t / g.nty) * g.nty;
-    const float* src = w.partial + w.part_off[sg] * (long long)(TILE_PX * CBLK);
-    for (int e = threadIdx.x; e < TILE_PX * CBLK; e += blockDim.x) {
-      float acc = 0.f;
-      for (int kc = 0; kc < nk; ++kc) acc += src[(long long)kc * TILE_PX * CBLK + e];
-      const int px = e / CBLK, cc = e % CBLK;
-      const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
-      const int c = cb * CBLK + cc;
-      if (i < g.nx && j < g.ny && c < g.nc) cube[((long long)i * g.ny + j) * g.nc + c] = acc;
-    }
+    const int tx = t / g.nty, ty = t - tx * g.nty;
+    const int px = e / width, c = cb * width + (e - px * width);
+    const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
+    if (i >= g.nx || j >= g.ny) continue;
+    float* dst = cube + ((long long)i * g.ny + j) * g.nc + c;
+    if (c < g.nc) dst[0] = acc.x;
+    if (c + 1 < g.nc) dst[1] = acc.y;
+    if (c + 2 < g.nc) dst[2] = acc.z;
+    if (c + 3 < g.nc) dst[3] = acc.w;
   }
+}
+
+void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms, cudaStream_t s) {
+  k_reduce_partials<<<num_sms * 8, RED_THREADS, 0, s>>>(g, w, cube);
 }
 
 // FP64 flux sums over the unpadded region: per-chunk partials, then a
@@ -248,7 +284,7 @@ void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, 
 void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
                           int num_sms, cudaStream_t s) {
   k_contract_fp32<<<num_sms * 2, F32_THREADS, 0, s>>>(g, w, spectra, cube);
-  k_reduce_partials<<<num_sms * 8, 256, 0, s>>>(g, w, cube);
+  launch_reduce_partials(g, w, cube, num_sms, s);
 }
 
 }  // namespace mg

@@ -147,6 +147,7 @@ void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float
                           int num_sms, cudaStream_t s);
 int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
                            int num_sms, cudaStream_t s);
+void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms, cudaStream_t s);
 void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, double* part,
                  double* flux, cudaStream_t s);
 int flux_chunks(int nx, int padx);

@@ -762,25 +762,6 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   }
 }
 
-// Split-K reduction for the tensor-core forms (full-band partial rows).
-__global__ void k_reduce_partials_tc(Geo g, Ws w, float* __restrict__ cube) {
-  if (w.hdr->status) return;
-  const int width = w.seg_width;
-  for (int t = blockIdx.x; t < w.nseg; t += gridDim.x) {
-    const int nk = w.seg_part[t];
-    if (nk == 0) continue;
-    const int tx = t / g.nty, ty = t - (t / g.nty) * g.nty;
-    const float* src = w.partial + w.part_off[t] * (long long)(TILE_PX * width);
-    for (int e = threadIdx.x; e < TILE_PX * width; e += blockDim.x) {
-      float acc = 0.f;
-      for (int kc = 0; kc < nk; ++kc) acc += src[(long long)kc * TILE_PX * width + e];
-      const int px = e / width, c = e % width;
-      const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
-      if (i < g.nx && j < g.ny && c < g.nc) cube[((long long)i * g.ny + j) * g.nc + c] = acc;
-    }
-  }
-}
-
 template <bool BF16, int KC>
 int launch_tc(const Geo& g, const Ws& w, const float* spectra, float* cube, int num_sms,
               cudaStream_t s, int nwmax) {
@@ -815,7 +796,7 @@ int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, floa
     rc = bf16 ? launch_tc<true, 32>(g, w, spectra, cube, num_sms, s, nwmax)
               : launch_tc<false, 32>(g, w, spectra, cube, num_sms, s, nwmax);
   if (rc) return rc;
-  k_reduce_partials_tc<<<num_sms * 8, 256, 0, s>>>(g, w, cube);
+  launch_reduce_partials(g, w, cube, num_sms, s);
   return MG_OK;
 }
 
