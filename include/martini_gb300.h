@@ -107,7 +107,8 @@ typedef struct mg_plan_info {
   int64_t n_items;          /* reserved (0) */
   int64_t n_partial_items;  /* upper bound on split-K partial tiles */
   int64_t n_tiles;
-  size_t workspace_bytes;   /* mg_workspace_size(p, n_pairs, n_partial_items) */
+  size_t workspace_bytes;   /* mg_workspace_size(p, n_pairs, n_partial_items), plus the
+                               spectrum store of the tensor-core forms (Gaussian lines) */
 } mg_plan_info;
 
 /* Library version string. */
@@ -141,7 +142,11 @@ int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* 
  * CUDA graph.  The workspace must have been sized by mg_workspace_size with
  * the same max_pairs / max_partial_items.  If the data need more than that,
  * the device code skips the contraction and mg_check() returns
- * MG_ERR_WORKSPACE.
+ * MG_ERR_WORKSPACE.  Bytes beyond mg_workspace_size(p, max_pairs,
+ * max_partial_items) hold the per-particle spectrum store of the tensor-core
+ * forms (Gaussian lines, computed once per particle instead of once per
+ * tile); mg_plan's workspace_bytes has room for it.  With less room the
+ * lines are evaluated inside the contraction: same results, slower.
  */
 int mg_insert(const mg_problem* p, void* workspace, size_t workspace_bytes, int64_t max_pairs,
               int64_t max_partial_items, void* stream);

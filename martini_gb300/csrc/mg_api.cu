@@ -235,6 +235,16 @@ int workspace_view(const mg_problem* p, const Geo& g, void* ws, size_t bytes,
     return fail(MG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(L.total) +
                                       " bytes, have " + std::to_string(bytes));
   *w = make_ws(ws, L, g.nc);
+  // the workspace beyond the fixed layout holds the spectrum store of the
+  // tensor-core forms (Gaussian lines); without room they evaluate in-kernel
+  if ((p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) &&
+      p->spectral_model == MG_SPECTRUM_GAUSSIAN) {
+    w->spec = reinterpret_cast<float*>(static_cast<char*>(ws) + L.total);
+    w->cap_spec = (long long)((bytes - L.total) / sizeof(float));
+  } else {
+    w->spec = nullptr;
+    w->cap_spec = 0;
+  }
   if (sort_bits(g, *w) > 32) return fail(MG_ERR_INVALID_ARGUMENT, "cube too large for the sort key");
   return MG_OK;
 }
@@ -287,7 +297,7 @@ int run(const mg_problem* p, void* ws, size_t bytes, cudaStream_t s, long long c
     if (e == cudaSuccess) e = cudaMemsetAsync(&w.hdr->item_counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return cuda_fail(e, "cube clear");
     if (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) {
-      rc = launch_contract_bf16x3(g, w, p->spectra, p->cube, num_sms(), s);
+      rc = launch_contract_bf16x3(g, w, p->n, p->spectra, p->cube, num_sms(), s);
       if (rc == MG_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tensor-core kernel set-up");
       if (rc) return fail(rc, "tensor-core form does not support this cube (band too wide)");
     } else {
@@ -324,8 +334,13 @@ int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* 
   info->n_items = 0;
   info->n_partial_items = h.partial_bound;
   info->n_tiles = g.ntiles;
+  size_t spec_bytes = 0;
+  if ((p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) &&
+      p->spectral_model == MG_SPECTRUM_GAUSSIAN)
+    spec_bytes = align256(sizeof(float) * (size_t)h.spec_bound);
   info->workspace_bytes = layout(p->n, g.ntiles, g.nc, p->form, flux_chunks(g.nx, g.padx),
-                                 h.n_pairs, h.partial_bound).total;
+                                 h.n_pairs, h.partial_bound).total +
+                          spec_bytes;
   return MG_OK;
 }
 

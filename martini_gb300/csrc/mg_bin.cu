@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) 
   extern __shared__ int s_count[];  // [ntiles] when the histogram is in shared memory
   __shared__ int s_wmax;
   __shared__ unsigned s_wb, s_sb;
+  __shared__ unsigned long long s_spec;
   const bool smem_hist = g.ntiles <= PREP_SMEM_TILES;
   const bool windows = w.ncb_seg > 1;
   if (smem_hist)
@@ -95,11 +96,13 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) 
   if (threadIdx.x == 0) {
     s_wmax = 0;
     s_wb = s_sb = 0u;
+    s_spec = 0ull;
   }
   __syncthreads();
   const int dec = w.hdr->edges_dec;
   int my_wmax = 0;
   unsigned my_wb = 0u, my_sb = 0u;
+  unsigned my_spec = 0u;  // support channels of this thread's particles
   // every thread of a block runs the same number of iterations
   for (long long base = blockIdx.x * (long long)blockDim.x; base < a.n;
        base += (long long)gridDim.x * blockDim.x) {
@@ -194,6 +197,7 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) 
           }
         }
       my_wmax = max(my_wmax, rec.chi - rec.clo);
+      my_spec += (unsigned)(rec.chi - rec.clo + 1);
       if (g.form == MG_FORM_F16X3) {
         // magnitude bounds for the scaled FP16 split (non-negative floats
         // order like their bit patterns)
@@ -213,14 +217,18 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) 
   my_wmax = __reduce_max_sync(0xffffffffu, my_wmax);
   my_wb = __reduce_max_sync(0xffffffffu, my_wb);
   my_sb = __reduce_max_sync(0xffffffffu, my_sb);
+  my_spec = __reduce_add_sync(0xffffffffu, my_spec);
   if ((threadIdx.x & 31) == 0) {
     atomicMax(&s_wmax, my_wmax);
     atomicMax(&s_wb, my_wb);
     atomicMax(&s_sb, my_sb);
+    atomicAdd(&s_spec, (unsigned long long)my_spec);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicMax(&w.hdr->wmax, s_wmax);
+    if (g.spectral_model == MG_SPECTRUM_GAUSSIAN)
+      atomicAdd(reinterpret_cast<unsigned long long*>(&w.hdr->spec_bound), s_spec);
     if (g.form == MG_FORM_F16X3) {
       atomicMax(&w.hdr->wbound_bits, s_wb);
       atomicMax(&w.hdr->sbound_bits, s_sb);
@@ -250,6 +258,8 @@ __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_part
     h->wbound_bits = 0u;
     h->sbound_bits = 0u;
     h->invw_bits = 0u;
+    h->spec_bound = 0;
+    h->n_spec = 0;
   }
 }
 

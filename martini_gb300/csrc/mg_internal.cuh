@@ -76,7 +76,9 @@ struct WsHeader {
   unsigned wbound_bits;          // max pixel weight bound (float bits, >= 0)
   unsigned sbound_bits;          // max spectrum bound (float bits, >= 0)
   unsigned invw_bits;            // max 1 / |channel width| (float bits)
-  long long pad1[4];
+  long long spec_bound;          // sum over particles of support channels (Gaussian)
+  long long n_spec;              // values in the spectrum store (contraction stage)
+  long long pad1[2];
 };
 
 // Pointers into the workspace (host computes, passes by value).  A
@@ -109,6 +111,8 @@ struct Ws {
   long long* part_off;   // [nseg] exclusive scan of seg_part
   float* partial;        // [cap_partial_items][TILE_PX][seg_width]
   double* flux_part;     // [flux_chunks][nc]
+  float* spec;           // [cap_spec] per-particle Gaussian spectra over [clo, chi]
+  long long cap_spec;    // room in spec (the workspace beyond the fixed layout)
   int nseg;              // ntiles * ncb_seg
   int ncb_seg;           // channel blocks per tile
   int seg_width;         // channels per segment (CBLK or nc rounded up to 16)
@@ -145,8 +149,8 @@ bool launch_radix_sort(unsigned* keys, int* vals, unsigned* kt, int* vt, const l
                        int num_sms, cudaStream_t s);
 void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
                           int num_sms, cudaStream_t s);
-int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
-                           int num_sms, cudaStream_t s);
+int launch_contract_bf16x3(const Geo& g, const Ws& w, long long n, const float* spectra,
+                           float* cube, int num_sms, cudaStream_t s);
 void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms, cudaStream_t s);
 void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, double* part,
                  double* flux, cudaStream_t s);

@@ -23,6 +23,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "mg_internal.cuh"
 
 namespace mg {
@@ -385,7 +387,7 @@ __device__ __forceinline__ void edge_term(const PRec& r, int ge, const float* eh
 // 0.5 [erf(b) - erf(a)] (a < b) from erfc(|a|), erfc(|b|) and the signs.
 __device__ __forceinline__ float half_diff_from_c(float ca, bool pa, float cb, bool pb) {
   const float both = 0.5f * (pa ? ca - cb : cb - ca);
-  return (pa || !pb) ? both : 1.f - 0.5f * (ca + cb);
+  return (pa || !pb) ? both : fmaf(-0.5f, ca + cb, 1.f);
 }
 
 // B = S for particles (q, q + 1) over the window channels.  A Gaussian line
@@ -398,9 +400,29 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
                                                const float* ehi, const float* elo,
                                                const float* inv_w, const float* spectra,
                                                int pid0, int pid1, int lane, float ss,
-                                               unsigned char* b_hi, unsigned char* b_lo) {
+                                               const float* spec, long long soff0,
+                                               long long soff1, unsigned char* b_hi,
+                                               unsigned char* b_lo) {
   const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
                         (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
+  if (spec) {
+    // Gaussian lines read from the spectrum store (rows over [clo, chi])
+    for (int base = 0; base < nw; base += 32) {  // warp-uniform
+      const int n = base + lane;
+      const int c = w0 + n;
+      float s0 = 0.f, s1 = 0.f;
+      if (v0 && c >= r0.clo && c <= r0.chi) s0 = __ldg(spec + soff0 + (c - r0.clo)) * ss;
+      if (v1 && c >= r1.clo && c <= r1.chi) s1 = __ldg(spec + soff1 + (c - r1.clo)) * ss;
+      if (n < nw) {
+        const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
+        unsigned hi, lo;
+        split_pair<BF16>(s0, s1, hi, lo);
+        *reinterpret_cast<unsigned*>(b_hi + off) = hi;
+        *reinterpret_cast<unsigned*>(b_lo + off) = lo;
+      }
+    }
+    return;
+  }
   const bool gauss = model == MG_SPECTRUM_GAUSSIAN;
   const int step = gauss ? 31 : 32;
   for (int base = 0; base < nw; base += step) {  // warp-uniform
@@ -448,6 +470,50 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
   }
 }
 
+// Row lengths of the spectrum store: support channels of each particle
+// that reaches the cube (0 otherwise).  Written over the per-particle pair
+// counts, which the binning stage no longer needs.
+__global__ void k_spec_count(long long n, Ws w) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const PRec& r = w.rec[p];
+    const int ilo = r.ilo, ihi = r.ihi, clo = r.clo, chi = r.chi;
+    w.npairs[p] = ilo <= ihi ? chi - clo + 1 : 0;
+  }
+}
+
+// Gaussian line of each particle over its support, once per particle (the
+// producer would otherwise evaluate it at every tile the particle touches):
+// one warp per particle, the same shared-edge arithmetic as the producer, so
+// the contraction gives the same bits with or without the store.  Row p
+// starts at pair_off[p] (exclusive scan of the row lengths).
+__global__ void k_spec_eval(long long n, int nc, Ws w) {
+  if (w.hdr->n_spec > w.cap_spec) return;
+  const int dec = w.hdr->edges_dec;
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; p < n;
+       p += nwarps) {
+    const int cnt = w.npairs[p];
+    if (cnt == 0) continue;  // warp-uniform
+    const PRec r = w.rec[p];
+    float* out = w.spec + w.pair_off[p];
+    for (int base = 0; base < cnt; base += 31) {
+      const int m = base + lane;
+      const int c = r.clo + m;
+      float ca = 0.f;
+      bool pa = true;
+      if (m <= cnt && c <= nc) edge_term(r, c, w.ehi, w.elo, ca, pa);
+      const float cb = __shfl_down_sync(0xffffffffu, ca, 1);
+      const bool pb = __shfl_down_sync(0xffffffffu, (int)pa, 1) != 0;
+      if (lane < 31 && m < cnt) {
+        const float phi = dec ? half_diff_from_c(cb, pb, ca, pa) : half_diff_from_c(ca, pa, cb, pb);
+        out[m] = r.amp * w.inv_w[c] * phi;
+      }
+    }
+  }
+}
+
 template <bool BF16, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict__ cube,
@@ -457,6 +523,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
+  __shared__ long long s_soff[2][KC];  // spectrum store rows
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[2 * KT_SMEM_CELLS];
   __shared__ __align__(8) unsigned long long bars[2];
@@ -469,6 +536,11 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   if (w.hdr->status) return;
   const long long n_items = w.hdr->n_items;
   const int dec = w.hdr->edges_dec;
+  // Gaussian lines come from the spectrum store when it was filled
+  const float* spec = (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 &&
+                       w.hdr->n_spec <= w.cap_spec)
+                          ? w.spec
+                          : nullptr;
 
   // exact power-of-two operand scales (FP16 form): largest |W|, |S| -> 2^14
   float sw = 1.f, ss = 1.f;
@@ -575,9 +647,11 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
         const int pid = w.list[it.lbeg + tid];
         recs[0][tid] = w.rec[pid];
         s_pid[0][tid] = pid;
+        s_soff[0][tid] = spec ? w.pair_off[pid] : 0;
       } else {
         recs[0][tid] = empty_rec();
         s_pid[0][tid] = 0;
+        s_soff[0][tid] = 0;
       }
     }
     __syncthreads();
@@ -595,11 +669,13 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
       // fetch the next stage's records while this one is produced
       PRec nrec;
       int npid = 0;
+      long long nsoff = 0;
       const bool has_next = ch + 1 < nchunk;
       if (has_next && tid < KC) {
         if (k0 + KC + tid < it.lcount) {
           npid = w.list[it.lbeg + k0 + KC + tid];
           nrec = w.rec[npid];
+          if (spec) nsoff = w.pair_off[npid];
         } else {
           nrec = empty_rec();
         }
@@ -641,11 +717,12 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
                              ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
         produce_s_pair<BF16>(r0, r1, v0, v1, q, w0, nw, g.nc, dec, g.spectral_model, w.ehi,
                              w.elo, w.inv_w, spectra, s_pid[buf][q], s_pid[buf][q + 1], lane,
-                             ss, sb_hi, sb_lo);
+                             ss, spec, s_soff[buf][q], s_soff[buf][q + 1], sb_hi, sb_lo);
       }
       if (has_next && tid < KC) {
         recs[buf ^ 1][tid] = nrec;
         s_pid[buf ^ 1][tid] = npid;
+        s_soff[buf ^ 1][tid] = nsoff;
       }
       fence_proxy_async();
       __syncthreads();
@@ -783,11 +860,18 @@ int launch_tc(const Geo& g, const Ws& w, const float* spectra, float* cube, int 
   return MG_OK;
 }
 
-int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
-                           int num_sms, cudaStream_t s) {
+int launch_contract_bf16x3(const Geo& g, const Ws& w, long long n, const float* spectra,
+                           float* cube, int num_sms, cudaStream_t s) {
   const int nwmax = w.seg_width;  // a stage window never exceeds the padded band
   if (nwmax > TC_TMEM_COLS) return MG_ERR_UNSUPPORTED;
   const bool bf16 = g.form == MG_FORM_BF16X3;
+  if (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 && n > 0) {
+    const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, (long long)num_sms * 16);
+    k_spec_count<<<blocks, 256, 0, s>>>(n, w);
+    launch_scan(w.npairs, n, w.pair_off, w.scan_sums, &w.hdr->n_spec, s);
+    const unsigned eblocks = (unsigned)std::min<long long>((n + 7) / 8, (long long)num_sms * 16);
+    k_spec_eval<<<eblocks, 256, 0, s>>>(n, g.nc, w);
+  }
   int rc;
   if (nwmax <= 256)
     rc = bf16 ? launch_tc<true, 64>(g, w, spectra, cube, num_sms, s, nwmax)

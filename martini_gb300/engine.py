@@ -110,10 +110,8 @@ class InsertionEngine:
         N.check(self.lib.mg_plan(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
                                  C.c_void_p(s.cuda_stream), C.byref(info)))
         self._caps = (int(info.n_pairs), int(info.n_partial_items))
-        need = C.c_size_t()
-        N.check(self.lib.mg_workspace_size(C.byref(prob), self._caps[0], self._caps[1],
-                                           C.byref(need)))
-        self._workspace(need.value)
+        # the plan's size includes the spectrum store of the tensor-core forms
+        self._workspace(int(info.workspace_bytes))
         self.last_plan = info
         return info
 

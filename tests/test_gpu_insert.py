@@ -247,3 +247,44 @@ def test_split_k_large_tile_matches_oracle(engine, form):
     ref = orc.insert_scatter(20, 24, x, y, ranges, kernels, kidx, h * resc, spectra)
     got, flux = run_gpu(engine, c, form=form)
     assert_close(got, ref, flux, tol=FORM_TOL[form])
+
+
+@pytest.mark.parametrize("form", [1, 2], ids=["bf16x3", "f16x3"])
+def test_spectrum_store_matches_in_kernel_lines(engine, form):
+    """The tensor-core forms read Gaussian lines from the per-particle
+    spectrum store when the workspace has room for it (mg_plan's size) and
+    evaluate them in the contraction otherwise (a workspace of exactly
+    mg_workspace_size).  Both use the same arithmetic: identical cubes."""
+    import ctypes as C
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    rng = np.random.default_rng(5)
+    n, nx, ny, nc = 4000, 48, 40, 96
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    h = 10 ** rng.uniform(-0.3, 0.8, n)
+    kidx, size, resc = orc.select_kernels(kernels, h)
+    parts = DeviceParticles.from_host(engine.device, rng.normal(24, 9, n), rng.normal(20, 8, n),
+                                      orc.sm_ranges(h, size), h * resc, kidx,
+                                      v=rng.normal(200, 60, n), sigma=rng.uniform(3, 20, n),
+                                      amp=10 ** rng.uniform(-7, -5, n))
+    edges = torch.from_numpy(orc.vrad_channel_edges(nc, 4.0, 200.0)).to(engine.device)
+    table = native_kernel_table(kernels)
+    s = C.c_void_p(torch.cuda.current_stream(engine.device).cuda_stream)
+    cubes = []
+    for with_store in (True, False):
+        cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=engine.device)
+        prob = engine.problem(parts, table, N.MG_SPECTRUM_GAUSSIAN, 0.0, nx, ny, nc, 0, 0, edges,
+                              cube, None, form)
+        info = engine.plan(prob)
+        exact = C.c_size_t()
+        N.check(engine.lib.mg_workspace_size(C.byref(prob), info.n_pairs, info.n_partial_items,
+                                             C.byref(exact)))
+        assert info.workspace_bytes > exact.value  # room for the store
+        nbytes = info.workspace_bytes if with_store else exact.value
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=engine.device)
+        N.check(engine.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), nbytes,
+                                     info.n_pairs, info.n_partial_items, s))
+        N.check(engine.lib.mg_check(C.c_void_p(ws.data_ptr()), s))
+        cubes.append(cube.cpu().numpy())
+    assert np.abs(cubes[0]).max() > 0
+    np.testing.assert_array_equal(cubes[0], cubes[1])
