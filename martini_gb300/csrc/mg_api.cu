@@ -45,15 +45,17 @@ int channel_bits(int nc) {
 }
 
 struct Layout {
-  size_t hdr, rec, npairs, pair_off, tile_count, tile_wlo, tile_whi, tile_off, ehi, elo, inv_w,
+  size_t hdr, rec, npairs, pair_off, tile_count, tile_diff, tile_wlo, tile_whi, tile_off, ehi, elo, inv_w,
       keys, list, keys_tmp, list_tmp, rs_hist, rs_off, scan_sums, seg_lo, seg_hi, seg_items,
       seg_part, item_off, part_off, partial, flux_part, total;
   int nseg, ncb, width;
 };
 
-Layout layout(long long n, int ntiles, int nc, int form, int flux_ch, long long cap_pairs,
+Layout layout(long long n, int nx, int ny, int nc, int form, int flux_ch, long long cap_pairs,
               long long cap_partial) {
   Layout L;
+  const int ntx = (nx + TILE_I - 1) / TILE_I, nty = (ny + TILE_J - 1) / TILE_J;
+  const int ntiles = ntx * nty;
   seg_shape(form, nc, &L.ncb, &L.width);
   L.nseg = ntiles * L.ncb;
   size_t o = 0;
@@ -73,6 +75,7 @@ Layout layout(long long n, int ntiles, int nc, int form, int flux_ch, long long 
   L.npairs = take(sizeof(int) * nn);
   L.pair_off = take(sizeof(long long) * nn);
   L.tile_count = take(sizeof(int) * ntiles);
+  L.tile_diff = take(sizeof(int) * (size_t)(ntx + 1) * (nty + 1));
   L.tile_wlo = take(sizeof(int) * ntiles);
   L.tile_whi = take(sizeof(int) * ntiles);
   L.tile_off = take(sizeof(long long) * (ntiles + 1));
@@ -106,6 +109,7 @@ Ws make_ws(void* base, const Layout& L, int nc) {
   w.npairs = reinterpret_cast<int*>(b + L.npairs);
   w.pair_off = reinterpret_cast<long long*>(b + L.pair_off);
   w.tile_count = reinterpret_cast<int*>(b + L.tile_count);
+  w.tile_diff = reinterpret_cast<int*>(b + L.tile_diff);
   w.tile_wlo = reinterpret_cast<int*>(b + L.tile_wlo);
   w.tile_whi = reinterpret_cast<int*>(b + L.tile_whi);
   w.tile_off = reinterpret_cast<long long*>(b + L.tile_off);
@@ -229,7 +233,7 @@ PrepArgs prep_args(const mg_problem* p) {
 
 int workspace_view(const mg_problem* p, const Geo& g, void* ws, size_t bytes,
                    long long cap_pairs, long long cap_partial, Ws* w) {
-  Layout L = layout(p->n, g.ntiles, g.nc, p->form, flux_chunks(g.nx, g.padx), cap_pairs,
+  Layout L = layout(p->n, g.nx, g.ny, g.nc, p->form, flux_chunks(g.nx, g.padx), cap_pairs,
                     cap_partial);
   if (!ws || bytes < L.total)
     return fail(MG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(L.total) +
@@ -266,8 +270,7 @@ int mg_workspace_size(const mg_problem* p, int64_t max_pairs, int64_t max_partia
     return fail(MG_ERR_INVALID_ARGUMENT, "invalid problem dimensions");
   if (max_pairs < 0 || max_partial_items < 0)
     return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
-  int ntiles = ((p->nx + TILE_I - 1) / TILE_I) * ((p->ny + TILE_J - 1) / TILE_J);
-  *bytes = layout(p->n, ntiles, p->nc, p->form, flux_chunks(p->nx, p->padx), max_pairs,
+  *bytes = layout(p->n, p->nx, p->ny, p->nc, p->form, flux_chunks(p->nx, p->padx), max_pairs,
                   max_partial_items).total;
   return MG_OK;
 }
@@ -338,7 +341,7 @@ int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* 
   if ((p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) &&
       p->spectral_model == MG_SPECTRUM_GAUSSIAN)
     spec_bytes = align256(sizeof(float) * (size_t)h.spec_bound);
-  info->workspace_bytes = layout(p->n, g.ntiles, g.nc, p->form, flux_chunks(g.nx, g.padx),
+  info->workspace_bytes = layout(p->n, g.nx, g.ny, g.nc, p->form, flux_chunks(g.nx, g.padx),
                                  h.n_pairs, h.partial_bound).total +
                           spec_bytes;
   return MG_OK;

@@ -76,23 +76,30 @@ __device__ __forceinline__ void channel_range(const double* e, int nc, int dec, 
 
 
 // One thread per particle: exact footprint, Dirac pixel, spectral support,
-// packed record.  The tile histogram is kept in shared memory when the tile
-// count fits (PREP_SMEM_TILES) and flushed once per block; the per-tile
-// channel windows (needed only when a tile has several channel blocks) and
-// the header maxima are reduced per block before their global atomics, so
-// no address sees one atomic per particle.
+// packed record.  Tile coverage goes into a 2D difference array over the
+// tile grid, (ntx + 1) x (nty + 1): +1 at the corners (tx0, ty0) and
+// (tx1 + 1, ty1 + 1), -1 at (tx0, ty1 + 1) and (tx1 + 1, ty0), so four
+// integer atomics per particle whatever its footprint; k_plan_tiles turns
+// it into exact per-tile counts with prefix sums.  The array lives in
+// shared memory when it fits (PREP_SMEM_DIFF) and is flushed once per block.
+// The per-tile channel windows (needed only when a tile has several channel
+// blocks) and the header maxima are reduced per block before their global
+// atomics.
 constexpr int PREP_THREADS = 256;
-constexpr int PREP_SMEM_TILES = 12288;
+constexpr int PREP_SMEM_DIFF = 12288;
 
 __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) {
-  extern __shared__ int s_count[];  // [ntiles] when the histogram is in shared memory
+  extern __shared__ int s_diff[];  // the difference array when it fits
   __shared__ int s_wmax;
   __shared__ unsigned s_wb, s_sb;
   __shared__ unsigned long long s_spec;
-  const bool smem_hist = g.ntiles <= PREP_SMEM_TILES;
+  const int dw = g.nty + 1;
+  const int ndiff = (g.ntx + 1) * dw;
+  const bool smem_hist = ndiff <= PREP_SMEM_DIFF;
+  int* const diff = smem_hist ? s_diff : w.tile_diff;
   const bool windows = w.ncb_seg > 1;
   if (smem_hist)
-    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x) s_count[t] = 0;
+    for (int t = threadIdx.x; t < ndiff; t += blockDim.x) s_diff[t] = 0;
   if (threadIdx.x == 0) {
     s_wmax = 0;
     s_wb = s_sb = 0u;
@@ -186,16 +193,17 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) 
       int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
       int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
       np = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
-      for (int tx = tx0; tx <= tx1; ++tx)
-        for (int ty = ty0; ty <= ty1; ++ty) {
-          int t = tx * g.nty + ty;
-          if (smem_hist) atomicAdd(&s_count[t], 1);
-          else atomicAdd(&w.tile_count[t], 1);
-          if (windows) {
+      atomicAdd(&diff[tx0 * dw + ty0], 1);
+      atomicAdd(&diff[tx0 * dw + ty1 + 1], -1);
+      atomicAdd(&diff[(tx1 + 1) * dw + ty0], -1);
+      atomicAdd(&diff[(tx1 + 1) * dw + ty1 + 1], 1);
+      if (windows)
+        for (int tx = tx0; tx <= tx1; ++tx)
+          for (int ty = ty0; ty <= ty1; ++ty) {
+            const int t = tx * g.nty + ty;
             atomicMin(&w.tile_wlo[t], rec.clo);
             atomicMax(&w.tile_whi[t], rec.chi);
           }
-        }
       my_wmax = max(my_wmax, rec.chi - rec.clo);
       my_spec += (unsigned)(rec.chi - rec.clo + 1);
       if (g.form == MG_FORM_F16X3) {
@@ -235,15 +243,18 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) 
     }
   }
   if (smem_hist)
-    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
-      if (s_count[t]) atomicAdd(&w.tile_count[t], s_count[t]);
+    for (int t = threadIdx.x; t < ndiff; t += blockDim.x)
+      if (s_diff[t]) atomicAdd(&w.tile_diff[t], s_diff[t]);
 }
 
 __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_partial) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.ntiles; t += gridDim.x * blockDim.x) {
-    w.tile_count[t] = 0;
-    w.tile_wlo[t] = 0x7fffffff;
-    w.tile_whi[t] = -1;
+  const int ndiff = (g.ntx + 1) * (g.nty + 1);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ndiff; t += gridDim.x * blockDim.x) {
+    w.tile_diff[t] = 0;
+    if (t < g.ntiles) {
+      w.tile_wlo[t] = 0x7fffffff;
+      w.tile_whi[t] = -1;
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     WsHeader* h = w.hdr;
@@ -263,13 +274,46 @@ __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_part
   }
 }
 
-// Single-block pass over tiles after the histogram: pair offsets of the
+// Single-block pass over tiles after the histogram: per-tile counts from the
+// difference array (prefix sums along ty, then along tx; in shared memory
+// when it fits in `smem_cap` ints, else in place), pair offsets of the
 // tile-major list and an upper bound on split-K partial items (every segment
 // of a tile holds at most the tile's count).
-__global__ void k_plan_tiles(Geo g, Ws w) {
+__global__ void k_plan_tiles(Geo g, Ws w, int smem_cap) {
   constexpr int NT = 1024;
   __shared__ long long s_a[NT], s_b[NT];
+  extern __shared__ int s_d[];
   const int tid = threadIdx.x;
+  {
+    const int dw = g.nty + 1, dh = g.ntx + 1;
+    const int ndiff = dw * dh;
+    const bool in_smem = ndiff <= smem_cap;
+    int* const d = in_smem ? s_d : w.tile_diff;
+    if (in_smem)
+      for (int e = tid; e < ndiff; e += NT) s_d[e] = w.tile_diff[e];
+    __syncthreads();
+    for (int r = tid; r < dh; r += NT) {
+      int acc = 0;
+      for (int c = 0; c < dw; ++c) {
+        acc += d[r * dw + c];
+        d[r * dw + c] = acc;
+      }
+    }
+    __syncthreads();
+    for (int c = tid; c < dw; c += NT) {
+      int acc = 0;
+      for (int r = 0; r < dh; ++r) {
+        acc += d[r * dw + c];
+        d[r * dw + c] = acc;
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < g.ntiles; t += NT) {
+      const int tx = t / g.nty, ty = t - tx * g.nty;
+      w.tile_count[t] = d[tx * dw + ty];
+    }
+    __syncthreads();
+  }
   const int per = (g.ntiles + NT - 1) / NT;
   const int t0 = tid * per;
   const int t1 = min(g.ntiles, t0 + per);
@@ -416,15 +460,26 @@ void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cuda
   if (a.n > 0) {
     // with the histogram in shared memory every block flushes up to ntiles
     // counts: fewer, longer-lived blocks
-    const bool smem_hist = g.ntiles <= PREP_SMEM_TILES;
-    const size_t hist_bytes = smem_hist ? sizeof(int) * (size_t)g.ntiles : 0;
+    const size_t ndiff = (size_t)(g.ntx + 1) * (g.nty + 1);
+    const bool smem_hist = ndiff <= (size_t)PREP_SMEM_DIFF;
+    const size_t hist_bytes = smem_hist ? sizeof(int) * ndiff : 0;
     unsigned blocks = grid_for(a.n, num_sms);
     const unsigned per_sm = hist_bytes <= 16384 ? 8u : 4u;
     if (smem_hist && blocks > per_sm * (unsigned)num_sms) blocks = per_sm * (unsigned)num_sms;
     k_prep<<<blocks, PREP_THREADS, hist_bytes, s>>>(a, g, w);
   }
   launch_scan(w.npairs, a.n, w.pair_off, w.scan_sums, nullptr, s);
-  k_plan_tiles<<<1, 1024, 0, s>>>(g, w);
+  // dynamic shared memory for the difference array: up to 200 KB
+  // (the attribute is per device: set on every launch, a host-side call)
+  constexpr int kPlanSmemCap = 50 * 1024;
+  const long long ndiff_all = (long long)(g.ntx + 1) * (g.nty + 1);
+  int cap = ndiff_all <= kPlanSmemCap ? (int)ndiff_all : 0;
+  if (cap > 0 && cudaFuncSetAttribute(k_plan_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(int) * kPlanSmemCap)) != cudaSuccess) {
+    cudaGetLastError();  // fall back to the in-place prefix sums
+    cap = 0;
+  }
+  k_plan_tiles<<<1, 1024, sizeof(int) * (size_t)cap, s>>>(g, w, cap);
 }
 
 int sort_bits(const Geo& g, const Ws& w) {

@@ -90,6 +90,7 @@ struct Ws {
   int* npairs;           // [n] tiles touched per particle
   long long* pair_off;   // [n] exclusive scan of npairs
   int* tile_count;       // [ntiles]
+  int* tile_diff;        // [(ntx + 1) * (nty + 1)] 2D difference array of tile coverage
   int* tile_wlo;         // [ntiles]
   int* tile_whi;         // [ntiles]
   long long* tile_off;   // [ntiles + 1] pair offsets (tile-major sorted list)

@@ -390,6 +390,12 @@ __device__ __forceinline__ float half_diff_from_c(float ca, bool pa, float cb, b
   return (pa || !pb) ? both : fmaf(-0.5f, ca + cb, 1.f);
 }
 
+// Spectrum store value of channel c for a particle (0 outside its support).
+__device__ __forceinline__ float spec_at(const float* spec, long long soff, const PRec& r, bool v,
+                                         int c) {
+  return (v && c >= r.clo && c <= r.chi) ? __ldg(spec + soff + (c - r.clo)) : 0.f;
+}
+
 // B = S for particles (q, q + 1) over the window channels.  A Gaussian line
 // needs erfc at every window edge once: in step m lane l evaluates edge
 // 31 m + l and channel 31 m + l (l < 31) takes its upper index edge from
@@ -401,18 +407,29 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
                                                const float* inv_w, const float* spectra,
                                                int pid0, int pid1, int lane, float ss,
                                                const float* spec, long long soff0,
-                                               long long soff1, unsigned char* b_hi,
-                                               unsigned char* b_lo) {
+                                               long long soff1, const float (&pf)[4],
+                                               unsigned char* b_hi, unsigned char* b_lo) {
   const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
                         (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
   if (spec) {
-    // Gaussian lines read from the spectrum store (rows over [clo, chi])
+    // Gaussian lines read from the spectrum store (rows over [clo, chi]);
+    // the first 64 window channels were loaded before the weights
     for (int base = 0; base < nw; base += 32) {  // warp-uniform
       const int n = base + lane;
       const int c = w0 + n;
-      float s0 = 0.f, s1 = 0.f;
-      if (v0 && c >= r0.clo && c <= r0.chi) s0 = __ldg(spec + soff0 + (c - r0.clo)) * ss;
-      if (v1 && c >= r1.clo && c <= r1.chi) s1 = __ldg(spec + soff1 + (c - r1.clo)) * ss;
+      float s0, s1;
+      if (base == 0) {
+        s0 = pf[0];
+        s1 = pf[1];
+      } else if (base == 32) {
+        s0 = pf[2];
+        s1 = pf[3];
+      } else {
+        s0 = spec_at(spec, soff0, r0, v0, c);
+        s1 = spec_at(spec, soff1, r1, v1, c);
+      }
+      s0 *= ss;
+      s1 *= ss;
       if (n < nw) {
         const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
         unsigned hi, lo;
@@ -713,11 +730,21 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
         const PRec r0 = recs[buf][q];
         const PRec r1 = recs[buf][q + 1];
         const bool v0 = q < kn, v1 = q + 1 < kn;
+        // spectrum store loads of the first 64 window channels, in flight
+        // while the weights are computed
+        float pf[4] = {0.f, 0.f, 0.f, 0.f};
+        if (spec) {
+          const long long so0 = s_soff[buf][q], so1 = s_soff[buf][q + 1];
+          pf[0] = spec_at(spec, so0, r0, v0, w0 + lane);
+          pf[1] = spec_at(spec, so1, r1, v1, w0 + lane);
+          pf[2] = spec_at(spec, so0, r0, v0, w0 + 32 + lane);
+          pf[3] = spec_at(spec, so1, r1, v1, w0 + 32 + lane);
+        }
         produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - 2 * (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
                              ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
         produce_s_pair<BF16>(r0, r1, v0, v1, q, w0, nw, g.nc, dec, g.spectral_model, w.ehi,
                              w.elo, w.inv_w, spectra, s_pid[buf][q], s_pid[buf][q + 1], lane,
-                             ss, spec, s_soff[buf][q], s_soff[buf][q + 1], sb_hi, sb_lo);
+                             ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf, sb_hi, sb_lo);
       }
       if (has_next && tid < KC) {
         recs[buf ^ 1][tid] = nrec;

@@ -288,3 +288,33 @@ def test_spectrum_store_matches_in_kernel_lines(engine, form):
         cubes.append(cube.cpu().numpy())
     assert np.abs(cubes[0]).max() > 0
     np.testing.assert_array_equal(cubes[0], cubes[1])
+
+
+@pytest.mark.parametrize("form", [0, 2], ids=["fp32", "f16x3"])
+@pytest.mark.parametrize("shape", [(2048, 2048), (4096, 2048)], ids=["2048x2048", "4096x2048"])
+def test_large_sparse_tile_grids(engine, shape, form):
+    """Tile grids too large for the shared-memory coverage histogram of the
+    binning kernel (2048 x 2048: 129 x 257 difference array) and for the
+    shared-memory prefix sums of the tile plan (4096 x 2048: 257 x 257)
+    take the global-memory paths: same cube as the oracle."""
+    nx, ny = shape
+    nc = 4
+    rng = np.random.default_rng(17)
+    n = 400
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    h = 10 ** rng.uniform(0.0, 1.3, n)
+    kidx, size, resc = orc.select_kernels(kernels, h)
+    x = rng.uniform(-10, nx + 10, n)
+    y = rng.uniform(-10, ny + 10, n)
+    edges = orc.vrad_channel_edges(nc, 4.0, 100.0)
+    sig = rng.uniform(3, 6, n)
+    v = rng.normal(100, 4, n)
+    mhi = 10 ** rng.uniform(4, 5, n)
+    dist = np.full(n, 3.0)
+    c = dict(x=x, y=y, ranges=orc.sm_ranges(h, size), h_eff=h * resc, kidx=kidx, v=v, sigma=sig,
+             amp=mhi / dist**2 / orc.MHI_TO_JY, kernels=kernels, spectral="gaussian",
+             edges=edges, nx=nx, ny=ny, nc=nc, pad=0)
+    spectra = orc.init_spectra("gaussian", mhi, dist, v, edges, sig)
+    ref = orc.insert_scatter(nx, ny, x, y, c["ranges"], kernels, kidx, c["h_eff"], spectra)
+    got, flux = run_gpu(engine, c, form=form)
+    assert_close(got, ref, flux, tol=FORM_TOL[form])
