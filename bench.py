@@ -34,10 +34,24 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "disc1m_512"
 METRIC = "cubes/s & particle-channel updates/s: FP32 vs BF16-split TC, <=1e-5 err vs FP64"
 L2_BYTES = 129 * 1024 * 1024
-# kernels of one mg_insert: tile init, edges, prep, 3 (pair scan), plan, emit,
-# 3 radix passes x (hist, 3 scan, scatter), segments, 2 x 3 (item scans),
-# partial check, contraction, split-K reduce, 2 flux
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 3 + 1 + 1 + 3 * 5 + 1 + 6 + 1 + 1 + 1 + 2
+# DRAM bytes (read + write) of one launch of the contraction kernel, from
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the full workload;
+# profiles/k_contract_tc_disc1m_512_f16x3.md gives the command and figures
+TRAFFIC_BYTES = {("disc1m_512", "f16x3"): 3_948_980_480}
+
+
+def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int) -> int:
+    """Kernels one mg_insert launches: tile init, edges, prep, pair scan (3),
+    plan, emit, radix passes x (histogram, scan (3), scatter), segments, item
+    and partial scans (2 x 3), partial check, [spectrum store: row lengths,
+    scan (3), rows], contraction, split-K reduction, flux (2)."""
+    ntiles = ((nx + 7) // 8) * ((ny + 15) // 16)  # 8 x 16-pixel tiles
+    bits = max(ntiles - 1, 0).bit_length() + max(nc - 1, 0).bit_length()
+    passes = (bits + 7) // 8
+    n = 1 + 1 + 1 + 3 + 1 + 1 + 5 * passes + 1 + 6 + 1
+    if form != "fp32" and gaussian:
+        n += 1 + 3 + 1
+    return n + 1 + 1 + 2
 
 
 def parse():
@@ -236,7 +250,7 @@ def main():
     eng.check()
 
     # --- dominant kernel: the contraction stage alone ------------------------
-    eng.run_stages(prob, N.MG_STAGE_BIN)
+    eng.run_stages(prob, N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
     cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(3)]
     for s, e in cev:
@@ -303,10 +317,7 @@ def main():
         pass
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     achieved_tf = flops / t_contract / 1e12
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", f"traffic_{a.workload}_{a.form}.json")
-    if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("bytes_per_launch")
+    traffic = TRAFFIC_BYTES.get((a.workload, a.form))
     line = {
         "metric": METRIC,
         "value": cubes_per_s,
@@ -328,13 +339,15 @@ def main():
         "particle_channel_updates_per_s": world * updates * a.steps / t_steps,
         "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf,
                      "unit": "TFLOP/s", "frac": achieved_tf / peak_tf, "traffic": traffic,
-                     "kernel": "k_contract (+ split-K reduce)",
+                     "kernel": ("k_contract_tc" if a.form != "fp32" else "k_contract_fp32")
+                     + " (stage timed: cube clear, contraction, split-K reduction)",
                      "contract_ms": t_contract * 1e3,
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks
                      else "fallback 1.9 PFLOP/s"},
         "e2e": {"value": world / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": LAUNCHES_PER_STEP * a.steps,
+        "gpu_launches": a.steps * launches_per_step(
+            a.form, w["spectral_model"] == N.MG_SPECTRUM_GAUSSIAN, nx, ny, nc),
         "step_ms": [round(s.elapsed_time(e), 3) for s, e in ev],
         "clocks": clk,
     }

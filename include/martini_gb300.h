@@ -155,11 +155,15 @@ int mg_insert(const mg_problem* p, void* workspace, size_t workspace_bytes, int6
 #define MG_STAGE_BIN 1        /* records, tile histogram, plan, tile-major list */
 #define MG_STAGE_CONTRACT 2   /* cube clear, contraction, split-K reduction */
 #define MG_STAGE_FLUX 4       /* FP64 flux sums (if p->flux) */
-#define MG_STAGE_ALL 7
+#define MG_STAGE_SPEC 8       /* per-particle spectrum store (tensor-core forms, Gaussian
+                                 lines; runs between BIN and CONTRACT; a BIN stage
+                                 invalidates it, and CONTRACT then evaluates in-kernel) */
+#define MG_STAGE_ALL 15
 
 /*
- * mg_insert restricted to some stages, in order, on the same workspace
- * (a stage reads what the previous ones left there).  For timing stages
+ * mg_insert restricted to some stages, in the order BIN, SPEC, CONTRACT,
+ * FLUX, on the same workspace (a stage reads what the previous ones left
+ * there).  For timing stages
  * separately; mg_insert == mg_insert_stages(..., MG_STAGE_ALL, ...).
  */
 int mg_insert_stages(const mg_problem* p, void* workspace, size_t workspace_bytes,

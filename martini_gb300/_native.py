@@ -47,7 +47,8 @@ MG_NOALLOC_SCRATCH_BYTES = 128 << 20
 MG_STAGE_BIN = 1
 MG_STAGE_CONTRACT = 2
 MG_STAGE_FLUX = 4
-MG_STAGE_ALL = 7
+MG_STAGE_SPEC = 8
+MG_STAGE_ALL = 15
 
 
 class KernelSpec(C.Structure):
@@ -126,3 +127,38 @@ def check(rc: int) -> None:
     if rc == MG_ERR_NOT_MONOTONIC:
         raise ValueError(msg)
     raise MartiniGB300Error(rc, msg)
+
+
+# SPH kernel classes (reference and mirror names, without the leading "_")
+_KERNEL_TYPES = {"WendlandC2Kernel": MG_KERNEL_WENDLAND_C2,
+                 "WendlandC6Kernel": MG_KERNEL_WENDLAND_C6,
+                 "CubicSplineKernel": MG_KERNEL_CUBIC_SPLINE,
+                 "QuarticSplineKernel": MG_KERNEL_QUARTIC_SPLINE,
+                 "GaussianKernel": MG_KERNEL_GAUSSIAN,
+                 "DiracDeltaKernel": MG_KERNEL_DIRAC}
+
+
+def kernel_table(kernel) -> list[tuple[int, float]]:
+    """(MG_KERNEL_*, truncate) rows for an SPH kernel object of the reference
+    (martini/sph_kernels.py) or of martini_gb300.sph_kernels: the sub-kernels
+    of an adaptive kernel in order (its ``kernels`` tuple, indexed by
+    ``kernel_indices``), or the single kernel."""
+    subs = getattr(kernel, "kernels", None) or (kernel,)
+    rows = []
+    for k in subs:
+        name = type(k).__name__.lstrip("_")
+        if name not in _KERNEL_TYPES:
+            raise ValueError(f"unsupported SPH kernel {type(k).__name__}")
+        t = _KERNEL_TYPES[name]
+        rows.append((t, float(getattr(k, "truncate", 0.0)) if t == MG_KERNEL_GAUSSIAN else 0.0))
+    if len(rows) > MG_MAX_KERNELS:
+        raise ValueError(f"at most {MG_MAX_KERNELS} kernels in an adaptive tuple")
+    return rows
+
+
+def set_kernels(p: "Problem", rows) -> None:
+    """Fill the kernel table of a Problem from kernel_table() rows."""
+    p.n_kernels = len(rows)
+    for k, (t, trunc) in enumerate(rows):
+        p.kernels[k].type = int(t)
+        p.kernels[k].truncate = float(trunc)

@@ -294,13 +294,15 @@ int run(const mg_problem* p, void* ws, size_t bytes, cudaStream_t s, long long c
     launch_prep(prep_args(p), g, w, num_sms(), s, cap_pairs, cap_partial);
     if (scatter) launch_sort_segments(prep_args(p), g, w, cap_pairs, num_sms(), s);
   }
+  if ((stages & MG_STAGE_SPEC) && (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3))
+    launch_spec_store(g, w, p->n, num_sms(), s);
   cudaError_t e;
   if (stages & MG_STAGE_CONTRACT) {
     e = cudaMemsetAsync(p->cube, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nc, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(&w.hdr->item_counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return cuda_fail(e, "cube clear");
     if (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) {
-      rc = launch_contract_bf16x3(g, w, p->n, p->spectra, p->cube, num_sms(), s);
+      rc = launch_contract_bf16x3(g, w, p->spectra, p->cube, num_sms(), s);
       if (rc == MG_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tensor-core kernel set-up");
       if (rc) return fail(rc, "tensor-core form does not support this cube (band too wide)");
     } else {

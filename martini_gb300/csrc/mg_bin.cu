@@ -271,6 +271,7 @@ __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_part
     h->invw_bits = 0u;
     h->spec_bound = 0;
     h->n_spec = 0;
+    h->spec_ready = 0;
   }
 }
 

@@ -77,8 +77,10 @@ struct WsHeader {
   unsigned sbound_bits;          // max spectrum bound (float bits, >= 0)
   unsigned invw_bits;            // max 1 / |channel width| (float bits)
   long long spec_bound;          // sum over particles of support channels (Gaussian)
-  long long n_spec;              // values in the spectrum store (contraction stage)
-  long long pad1[2];
+  long long n_spec;              // values in the spectrum store (spectrum stage)
+  int spec_ready;                // 1 once the store holds this binning's spectra
+  int pad2;
+  long long pad1[1];
 };
 
 // Pointers into the workspace (host computes, passes by value).  A
@@ -150,9 +152,10 @@ bool launch_radix_sort(unsigned* keys, int* vals, unsigned* kt, int* vt, const l
                        int num_sms, cudaStream_t s);
 void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
                           int num_sms, cudaStream_t s);
-int launch_contract_bf16x3(const Geo& g, const Ws& w, long long n, const float* spectra,
-                           float* cube, int num_sms, cudaStream_t s);
+int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
+                           int num_sms, cudaStream_t s);
 void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms, cudaStream_t s);
+void launch_spec_store(const Geo& g, const Ws& w, long long n, int num_sms, cudaStream_t s);
 void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, double* part,
                  double* flux, cudaStream_t s);
 int flux_chunks(int nx, int padx);

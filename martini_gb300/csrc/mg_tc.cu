@@ -505,7 +505,10 @@ __global__ void k_spec_count(long long n, Ws w) {
 // the contraction gives the same bits with or without the store.  Row p
 // starts at pair_off[p] (exclusive scan of the row lengths).
 __global__ void k_spec_eval(long long n, int nc, Ws w) {
-  if (w.hdr->n_spec > w.cap_spec) return;
+  const bool fits = w.hdr->n_spec <= w.cap_spec;
+  // read by the contraction, which runs after this whole kernel
+  if (blockIdx.x == 0 && threadIdx.x == 0) w.hdr->spec_ready = fits ? 1 : 0;
+  if (!fits) return;
   const int dec = w.hdr->edges_dec;
   const int lane = threadIdx.x & 31;
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -555,7 +558,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   const int dec = w.hdr->edges_dec;
   // Gaussian lines come from the spectrum store when it was filled
   const float* spec = (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 &&
-                       w.hdr->n_spec <= w.cap_spec)
+                       w.hdr->spec_ready)
                           ? w.spec
                           : nullptr;
 
@@ -887,18 +890,22 @@ int launch_tc(const Geo& g, const Ws& w, const float* spectra, float* cube, int 
   return MG_OK;
 }
 
-int launch_contract_bf16x3(const Geo& g, const Ws& w, long long n, const float* spectra,
-                           float* cube, int num_sms, cudaStream_t s) {
+// Spectrum store of the tensor-core forms (Gaussian lines): row lengths,
+// their scan into row offsets, the rows.
+void launch_spec_store(const Geo& g, const Ws& w, long long n, int num_sms, cudaStream_t s) {
+  if (g.spectral_model != MG_SPECTRUM_GAUSSIAN || w.cap_spec <= 0 || n <= 0) return;
+  const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, (long long)num_sms * 16);
+  k_spec_count<<<blocks, 256, 0, s>>>(n, w);
+  launch_scan(w.npairs, n, w.pair_off, w.scan_sums, &w.hdr->n_spec, s);
+  const unsigned eblocks = (unsigned)std::min<long long>((n + 7) / 8, (long long)num_sms * 16);
+  k_spec_eval<<<eblocks, 256, 0, s>>>(n, g.nc, w);
+}
+
+int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
+                           int num_sms, cudaStream_t s) {
   const int nwmax = w.seg_width;  // a stage window never exceeds the padded band
   if (nwmax > TC_TMEM_COLS) return MG_ERR_UNSUPPORTED;
   const bool bf16 = g.form == MG_FORM_BF16X3;
-  if (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 && n > 0) {
-    const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, (long long)num_sms * 16);
-    k_spec_count<<<blocks, 256, 0, s>>>(n, w);
-    launch_scan(w.npairs, n, w.pair_off, w.scan_sums, &w.hdr->n_spec, s);
-    const unsigned eblocks = (unsigned)std::min<long long>((n + 7) / 8, (long long)num_sms * 16);
-    k_spec_eval<<<eblocks, 256, 0, s>>>(n, g.nc, w);
-  }
   int rc;
   if (nwmax <= 256)
     rc = bf16 ? launch_tc<true, 64>(g, w, spectra, cube, num_sms, s, nwmax)

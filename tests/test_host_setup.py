@@ -155,3 +155,18 @@ def test_thermal_width_known_answer():
 def test_gaussian_truncation_below_two_raises():
     with pytest.raises(RuntimeError, match="truncation <2sigma"):
         K._GaussianKernel(truncate=1.0)
+
+
+def test_kernel_table_of_adaptive_and_single_kernels():
+    """kernel_table maps kernel objects to the C ABI's rows, adaptive tuples in
+    order (WendlandC2 -> Dirac -> Gaussian(6), sph_kernels.py:1629-1635)."""
+    from martini_gb300 import _native as N
+    from martini_gb300 import sph_kernels as K
+    rows = N.kernel_table(K.WendlandC2Kernel())
+    assert rows == [(N.MG_KERNEL_WENDLAND_C2, 0.0), (N.MG_KERNEL_DIRAC, 0.0),
+                    (N.MG_KERNEL_GAUSSIAN, 6.0)]
+    assert N.kernel_table(K.DiracDeltaKernel()) == [(N.MG_KERNEL_DIRAC, 0.0)]
+    p = N.Problem()
+    N.set_kernels(p, rows)
+    assert p.n_kernels == 3 and p.kernels[2].type == N.MG_KERNEL_GAUSSIAN
+    assert abs(p.kernels[2].truncate - 6.0) < 1e-6
