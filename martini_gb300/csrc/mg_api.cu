@@ -27,11 +27,19 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Segment shape of a contraction form: channel blocks per tile and their width.
+// Segment shape of a contraction form: channel blocks per tile and their
+// width.  Tensor-core forms: the band (rounded to 16) in one block up to 256
+// channels, else blocks of 256 (a block and its master accumulator fill the
+// 512 TMEM columns).
 void seg_shape(int form, int nc, int* ncb, int* width) {
   if (form == MG_FORM_BF16X3 || form == MG_FORM_F16X3) {
-    *ncb = 1;
-    *width = (nc + 15) / 16 * 16;
+    if (nc <= 256) {
+      *ncb = 1;
+      *width = (nc + 15) / 16 * 16;
+    } else {
+      *ncb = (nc + 255) / 256;
+      *width = 256;
+    }
   } else {
     *ncb = (nc + CBLK - 1) / CBLK;
     *width = CBLK;

@@ -280,7 +280,7 @@ __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_part
 // when it fits in `smem_cap` ints, else in place), pair offsets of the
 // tile-major list and an upper bound on split-K partial items (every segment
 // of a tile holds at most the tile's count).
-__global__ void k_plan_tiles(Geo g, Ws w, int smem_cap) {
+__global__ void k_plan_tiles(Geo g, Ws w, int smem_cap, int num_sms) {
   constexpr int NT = 1024;
   __shared__ long long s_a[NT], s_b[NT];
   extern __shared__ int s_d[];
@@ -319,21 +319,27 @@ __global__ void k_plan_tiles(Geo g, Ws w, int smem_cap) {
   const int t0 = tid * per;
   const int t1 = min(g.ntiles, t0 + per);
   long long sa = 0, sb = 0;
-  for (int t = t0; t < t1; ++t) {
-    int cnt = w.tile_count[t];
-    sa += cnt;
-    int nk = (cnt + KCH - 1) / KCH;
-    if (nk > 1) sb += (long long)nk * w.ncb_seg;
-  }
+  for (int t = t0; t < t1; ++t) sa += w.tile_count[t];
   s_a[tid] = sa;
-  s_b[tid] = sb;
   __syncthreads();
   for (int off = 1; off < NT; off <<= 1) {
-    long long a = 0, b = 0;
-    if (tid >= off) { a = s_a[tid - off]; b = s_b[tid - off]; }
+    long long a = 0;
+    if (tid >= off) a = s_a[tid - off];
     __syncthreads();
     s_a[tid] += a;
-    s_b[tid] += b;
+    __syncthreads();
+  }
+  // item size from the total, then the split-K bound with it
+  const int kch = item_particles(s_a[NT - 1], num_sms);
+  for (int t = t0; t < t1; ++t) {
+    const int cnt = w.tile_count[t];
+    const int nk = (cnt + kch - 1) / kch;
+    if (nk > 1) sb += (long long)nk * w.ncb_seg;
+  }
+  s_b[tid] = sb;
+  __syncthreads();
+  for (int off = NT / 2; off > 0; off >>= 1) {
+    if (tid < off) s_b[tid] += s_b[tid + off];
     __syncthreads();
   }
   long long ea = s_a[tid] - sa;
@@ -345,7 +351,8 @@ __global__ void k_plan_tiles(Geo g, Ws w, int smem_cap) {
     w.tile_off[g.ntiles] = s_a[NT - 1];
     WsHeader* h = w.hdr;
     h->n_pairs = s_a[NT - 1];
-    h->partial_bound = s_b[NT - 1];
+    h->partial_bound = s_b[0];
+    h->kch = kch;
     unsigned st = h->status & ST_EDGES;
     if (h->n_pairs > h->cap_pairs) st |= ST_PAIRS;
     h->status = st;
@@ -388,6 +395,7 @@ __device__ __forceinline__ long long lower_bound_keys(const unsigned* keys, long
 __global__ void k_segments(Geo g, Ws w) {
   const bool bad = (w.hdr->status & (ST_PAIRS | ST_EDGES)) != 0;
   const int wmax = w.hdr->wmax;
+  const int kch = w.hdr->kch;
   const unsigned cmask_hi = (1u << w.cbits);
   for (int sg = blockIdx.x * blockDim.x + threadIdx.x; sg < w.nseg; sg += gridDim.x * blockDim.x) {
     const int t = sg / w.ncb_seg;
@@ -412,7 +420,7 @@ __global__ void k_segments(Geo g, Ws w) {
       }
       const long long cnt = hi - lo;
       if (cnt > 0) {
-        items = (int)((cnt + KCH - 1) / KCH);
+        items = (int)((cnt + kch - 1) / kch);
         part = items > 1 ? items : 0;
       }
     }
@@ -480,7 +488,7 @@ void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cuda
     cudaGetLastError();  // fall back to the in-place prefix sums
     cap = 0;
   }
-  k_plan_tiles<<<1, 1024, sizeof(int) * (size_t)cap, s>>>(g, w, cap);
+  k_plan_tiles<<<1, 1024, sizeof(int) * (size_t)cap, s>>>(g, w, cap, num_sms);
 }
 
 int sort_bits(const Geo& g, const Ws& w) {

@@ -30,7 +30,8 @@ struct ItemInfo {
   int lcount;
 };
 
-__device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long long item) {
+__device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long long item,
+                                                int kch) {
   ItemInfo it;
   const int sg = find_segment(w.item_off, w.nseg, item);
   it.seg = sg;
@@ -41,9 +42,9 @@ __device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long 
   it.nk = w.seg_items[sg];
   it.kc = (int)(item - w.item_off[sg]);
   it.c0 = cb * w.seg_width;
-  it.lbeg = w.seg_lo[sg] + (long long)it.kc * KCH;
+  it.lbeg = w.seg_lo[sg] + (long long)it.kc * kch;
   const long long left = w.seg_hi[sg] - it.lbeg;
-  it.lcount = (int)(left < KCH ? left : KCH);
+  it.lcount = (int)(left < kch ? left : kch);
   return it;
 }
 
@@ -60,6 +61,7 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
   const WsHeader* hdr = w.hdr;
   if (hdr->status) return;
   const long long n_items = hdr->n_items;
+  const int kch = hdr->kch;
   const int dec = hdr->edges_dec;
   const int tr = tid >> 4;  // pixel group: pixels tr*8 .. tr*8+7
   const int tc = tid & 15;  // channel group: channels tc*4 .. tc*4+3
@@ -70,7 +72,7 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
     const long long item = s_item;
     __syncthreads();
     if (item >= n_items) break;
-    const ItemInfo it = decode_item(g, w, item);
+    const ItemInfo it = decode_item(g, w, item, kch);
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
 
     float acc[8][4];
@@ -219,9 +221,11 @@ void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms,
   k_reduce_partials<<<num_sms * 8, RED_THREADS, 0, s>>>(g, w, cube);
 }
 
-// FP64 flux sums over the unpadded region: per-chunk partials, then a
-// fixed-order final reduction (martini/martini.py:367-392).
-constexpr int FLUX_ROWS = 8;  // pixel rows (axis 0) per chunk
+// FP64 flux sums over the unpadded region (martini/martini.py:367-392):
+// every voxel is widened to FP64 and added in a fixed order, per pixel row
+// (one block per row of the unpadded region, a thread per channel), then
+// the row sums in row order.
+constexpr int FLUX_ROWS = 1;  // pixel rows (axis 0) per chunk
 
 __global__ void k_flux_partial(const float* __restrict__ cube, int nx, int ny, int nc, int padx,
                                int pady, double* __restrict__ part) {
@@ -232,17 +236,7 @@ __global__ void k_flux_partial(const float* __restrict__ cube, int nx, int ny, i
     double acc = 0.0;
     for (int i = i0; i < i1; ++i) {
       const float* row = cube + ((long long)i * ny) * nc + c;
-      float f = 0.f;
-      int cnt = 0;
-      for (int j = pady; j < ny - pady; ++j) {
-        f += row[(long long)j * nc];
-        if (++cnt == 8) {
-          acc += (double)f;
-          f = 0.f;
-          cnt = 0;
-        }
-      }
-      acc += (double)f;
+      for (int j = pady; j < ny - pady; ++j) acc += (double)__ldcs(row + (long long)j * nc);
     }
     part[(long long)chunk * nc + c] = acc;
   }

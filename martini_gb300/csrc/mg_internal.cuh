@@ -18,7 +18,21 @@ constexpr int TILE_I = 8;    // pixels along axis 0 (RA index)
 constexpr int TILE_J = 16;   // pixels along axis 1 (Dec index)
 constexpr int TILE_PX = TILE_I * TILE_J;
 constexpr int CBLK = 64;     // channels per FP32 work item
-constexpr int KCH = 2048;    // particles per work item (split-K granularity)
+constexpr int KCH_MIN = 2048;     // fewest particles per work item (split-K granularity)
+constexpr int ITEMS_PER_SM = 24;  // target work items per SM when the pairs allow
+
+// Particles per work item for a launch with `total_pairs` (tile, particle)
+// pairs: about ITEMS_PER_SM items per SM, a multiple of 64, at least
+// KCH_MIN.  Small problems keep fine items for load balance; large ones get
+// items long enough that split-K partial tiles stay few.
+__host__ __device__ inline int item_particles(long long total_pairs, int num_sms) {
+  const long long per = (long long)(num_sms > 0 ? num_sms : 1) * ITEMS_PER_SM;
+  long long t = (total_pairs + per - 1) / per;
+  t = (t + 63) / 64 * 64;
+  if (t < KCH_MIN) t = KCH_MIN;
+  if (t > (1LL << 30)) t = 1LL << 30;
+  return (int)t;
+}
 
 // Per-particle record written by the prep kernel (64 bytes).
 struct PRec {
@@ -79,7 +93,7 @@ struct WsHeader {
   long long spec_bound;          // sum over particles of support channels (Gaussian)
   long long n_spec;              // values in the spectrum store (spectrum stage)
   int spec_ready;                // 1 once the store holds this binning's spectra
-  int pad2;
+  int kch;                       // particles per work item (item_particles)
   long long pad1[1];
 };
 

@@ -213,26 +213,29 @@ __device__ __forceinline__ float tc_spectrum(const PRec& r, int model, int c, in
 }
 
 struct ItemTC {
-  int tile, tx, ty, kc, nk;
+  int seg, tile, tx, ty, kc, nk;
+  int c0;  // first channel of the segment's block
   long long lbeg;
   int lcount;
 };
 
-__device__ __forceinline__ ItemTC decode_tc(const Geo& g, const Ws& w, long long item) {
+__device__ __forceinline__ ItemTC decode_tc(const Geo& g, const Ws& w, long long item, int kch) {
   int a = 0, b = w.nseg;
   while (b - a > 1) {
     int m = (a + b) >> 1;
     if (w.item_off[m] <= item) a = m; else b = m;
   }
   ItemTC it;
-  it.tile = a;  // one segment per tile in this form
-  it.tx = a / g.nty;
-  it.ty = a - it.tx * g.nty;
+  it.seg = a;
+  it.tile = a / w.ncb_seg;
+  it.c0 = (a - it.tile * w.ncb_seg) * w.seg_width;
+  it.tx = it.tile / g.nty;
+  it.ty = it.tile - it.tx * g.nty;
   it.nk = w.seg_items[a];
   it.kc = (int)(item - w.item_off[a]);
-  it.lbeg = w.seg_lo[a] + (long long)it.kc * KCH;
+  it.lbeg = w.seg_lo[a] + (long long)it.kc * kch;
   const long long left = w.seg_hi[a] - it.lbeg;
-  it.lcount = (int)(left < KCH ? left : KCH);
+  it.lcount = (int)(left < kch ? left : kch);
   return it;
 }
 
@@ -555,6 +558,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   const int warp = tid >> 5, lane = tid & 31;
   if (w.hdr->status) return;
   const long long n_items = w.hdr->n_items;
+  const int kch = w.hdr->kch;
   const int dec = w.hdr->edges_dec;
   // Gaussian lines come from the spectrum store when it was filled
   const float* spec = (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 &&
@@ -614,7 +618,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   const int quarter = warp & 3;    // TMEM lane quarter of this warp
   const int colgrp = warp >> 2;    // 4 warps share a quarter: 32-column groups
   const unsigned lane_base = (unsigned)(quarter * 32) << 16;
-  const int ncols = w.seg_width;   // channels held in TMEM (nc rounded to 16)
+  const int ncols = w.seg_width;   // channels of a segment's block held in TMEM (<= 256)
 
   const bool drain = ncols <= TC_MASTER_COL;  // master accumulator fits
   auto zero_tmem = [&]() {
@@ -657,7 +661,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
     __syncthreads();
     const long long item = s_item;
     if (item >= n_items || s_abort) break;
-    const ItemTC it = decode_tc(g, w, item);
+    const ItemTC it = decode_tc(g, w, item, kch);
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
     const int nchunk = (it.lcount + KC - 1) / KC;
 
@@ -713,6 +717,10 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
           lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
           hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
         }
+        // relative to the segment's block [c0, c0 + ncols)
+        lo = max(lo, it.c0) - it.c0;
+        hi = min(hi, it.c0 + ncols - 1) - it.c0;
+        if (hi < lo) lo = hi = 0;  // no support in this block: zeros
         w0 = lo & ~15;
         nw = ((hi + 1 - w0) + 15) & ~15;
         if (nw < 16) nw = 16;
@@ -738,14 +746,15 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
         float pf[4] = {0.f, 0.f, 0.f, 0.f};
         if (spec) {
           const long long so0 = s_soff[buf][q], so1 = s_soff[buf][q + 1];
-          pf[0] = spec_at(spec, so0, r0, v0, w0 + lane);
-          pf[1] = spec_at(spec, so1, r1, v1, w0 + lane);
-          pf[2] = spec_at(spec, so0, r0, v0, w0 + 32 + lane);
-          pf[3] = spec_at(spec, so1, r1, v1, w0 + 32 + lane);
+          const int wa = it.c0 + w0;
+          pf[0] = spec_at(spec, so0, r0, v0, wa + lane);
+          pf[1] = spec_at(spec, so1, r1, v1, wa + lane);
+          pf[2] = spec_at(spec, so0, r0, v0, wa + 32 + lane);
+          pf[3] = spec_at(spec, so1, r1, v1, wa + 32 + lane);
         }
         produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - 2 * (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
                              ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
-        produce_s_pair<BF16>(r0, r1, v0, v1, q, w0, nw, g.nc, dec, g.spectral_model, w.ehi,
+        produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, g.nc, dec, g.spectral_model, w.ehi,
                              w.elo, w.inv_w, spectra, s_pid[buf][q], s_pid[buf][q + 1], lane,
                              ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf, sb_hi, sb_lo);
       }
@@ -816,15 +825,17 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
       const bool inside = i < g.nx && j < g.ny;
       float* dst;
       int limit;
+      bool vec;
       if (it.nk == 1) {
-        dst = cube + ((long long)i * g.ny + j) * g.nc;
-        limit = g.nc;
+        dst = cube + ((long long)i * g.ny + j) * g.nc + it.c0;
+        limit = min(ncols, g.nc - it.c0);
+        vec = (g.nc & 3) == 0 && (limit & 3) == 0;  // 16-byte aligned rows
       } else {
-        const long long slot = w.part_off[it.tile] + it.kc;
+        const long long slot = w.part_off[it.seg] + it.kc;
         dst = w.partial + (slot * TILE_PX + p) * (long long)ncols;
         limit = ncols;
+        vec = true;
       }
-      const bool vec = ((limit & 3) == 0);
       for (int c = colgrp * 32; c < ncols; c += 128) {
         unsigned r[32];
         tmem_ld32(tmem + lane_base + (unsigned)c, r);
@@ -903,16 +914,12 @@ void launch_spec_store(const Geo& g, const Ws& w, long long n, int num_sms, cuda
 
 int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
                            int num_sms, cudaStream_t s) {
-  const int nwmax = w.seg_width;  // a stage window never exceeds the padded band
-  if (nwmax > TC_TMEM_COLS) return MG_ERR_UNSUPPORTED;
+  const int nwmax = w.seg_width;  // a stage window never exceeds the segment's block
+  if (nwmax > TC_MASTER_COL) return MG_ERR_UNSUPPORTED;
   const bool bf16 = g.form == MG_FORM_BF16X3;
   int rc;
-  if (nwmax <= 256)
-    rc = bf16 ? launch_tc<true, 64>(g, w, spectra, cube, num_sms, s, nwmax)
-              : launch_tc<false, 64>(g, w, spectra, cube, num_sms, s, nwmax);
-  else
-    rc = bf16 ? launch_tc<true, 32>(g, w, spectra, cube, num_sms, s, nwmax)
-              : launch_tc<false, 32>(g, w, spectra, cube, num_sms, s, nwmax);
+  rc = bf16 ? launch_tc<true, 64>(g, w, spectra, cube, num_sms, s, nwmax)
+            : launch_tc<false, 64>(g, w, spectra, cube, num_sms, s, nwmax);
   if (rc) return rc;
   launch_reduce_partials(g, w, cube, num_sms, s);
   return MG_OK;

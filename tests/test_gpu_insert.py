@@ -318,3 +318,33 @@ def test_large_sparse_tile_grids(engine, shape, form):
     ref = orc.insert_scatter(nx, ny, x, y, c["ranges"], kernels, kidx, c["h_eff"], spectra)
     got, flux = run_gpu(engine, c, form=form)
     assert_close(got, ref, flux, tol=FORM_TOL[form])
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+@pytest.mark.parametrize("nc", [300, 512])
+def test_wide_band(engine, form, nc):
+    """Bands wider than 256 channels (the 2 km/s, 512-channel configuration):
+    the tensor-core forms hold the whole band in TMEM (KC = 32 stages, no
+    master accumulator); the FP32 form uses many 64-channel blocks."""
+    g = orc.disc_particles(6000, seed=33, h_med=0.7)
+    xyz, vxyz = orc.incline(g["xyz"], g["vxyz"], 60.0)
+    ra, dec, v, d = orc.project_particles(xyz, vxyz, 10.0)
+    x, y = orc.tan_world2pix(ra, dec, 0.0, 0.0, 32.5, 32.5, -10 / 3600, 10 / 3600)
+    hpx = orc.sm_lengths_px(g["hsm"], d, 10.0)
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    kidx, size, resc = orc.select_kernels(kernels, hpx)
+    ranges = orc.sm_ranges(hpx, size)
+    vc = 700.0
+    edges = orc.vrad_channel_edges(nc, 2.0, vc)
+    sig = orc.thermal_sigma_kms(g["T"])
+    vchan = (nc - 1) / 2 + (v - vc) / -2.0
+    keep = orc.prune_mask(x, y, vchan, ranges, g["mHI"], 64, 64, nc, sig, edges)
+    c = dict(x=x[keep], y=y[keep], ranges=ranges[keep], h_eff=(hpx * resc)[keep],
+             kidx=kidx[keep], v=v[keep], sigma=sig[keep],
+             amp=(g["mHI"] / d**2 / orc.MHI_TO_JY)[keep], kernels=kernels, spectral="gaussian",
+             edges=edges, nx=64, ny=64, nc=nc, pad=0)
+    spectra = orc.init_spectra("gaussian", g["mHI"][keep], d[keep], v[keep], edges, sig[keep])
+    ref = orc.insert_scatter(64, 64, c["x"], c["y"], c["ranges"], kernels, c["kidx"],
+                             c["h_eff"], spectra)
+    got, flux = run_gpu(engine, c, form=form)
+    assert_close(got, ref, flux, tol=FORM_TOL[form])
