@@ -204,21 +204,31 @@ def main():
     torch.cuda.set_device(dev)
     w = workloads.build(a.workload, n=a.n)
     form = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}[a.form]
-    eng = InsertionEngine(dev)
-    parts = DeviceParticles.from_host(dev, w["x"], w["y"], w["sm_range"], w["h_eff"],
-                                      w["kernel_index"], v=w["v"], sigma=w["sigma"], amp=w["amp"])
     edges = torch.from_numpy(np.ascontiguousarray(w["edges"])).to(dev)
     nx, ny, nc = w["nx"], w["ny"], w["nc"]
     cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=dev)
     flux = torch.empty(nc + 1, dtype=torch.float64, device=dev)
-    prob = eng.problem(parts, w["kernels"], w["spectral_model"], w["sigma_const"], nx, ny, nc, 0,
-                       0, edges, cube, flux, form)
-    info = eng.plan(prob)
+    # one insertion per spectral group; later groups add to the cube
+    groups = w["groups"] or [dict(sel=None, spectral_model=w["spectral_model"])]
+    ins = []
+    for gi, grp in enumerate(groups):
+        s = slice(None) if grp["sel"] is None else grp["sel"]
+        kidx = w["kernel_index"][s] if w["kernel_index"] is not None else None
+        sig = w["sigma"][s] if w["sigma"] is not None else None
+        eng = InsertionEngine(dev)
+        parts = DeviceParticles.from_host(dev, w["x"][s], w["y"][s], w["sm_range"][s],
+                                          w["h_eff"][s], kidx, v=w["v"][s], sigma=sig,
+                                          amp=w["amp"][s])
+        prob = eng.problem(parts, w["kernels"], grp["spectral_model"], w["sigma_const"], nx, ny,
+                           nc, 0, 0, edges, cube, flux, form, accumulate=gi > 0)
+        info = eng.plan(prob)
+        ins.append(dict(eng=eng, parts=parts, prob=prob, info=info, s=s))
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
     def step():
-        eng.run(prob)
+        for g in ins:
+            g["eng"].run(g["prob"])
 
     # the clock sampler starts before the warm-up: nvidia-smi's start-up
     # stalls the GPU for a moment and must not fall into the timed region
@@ -229,7 +239,8 @@ def main():
         flush.zero_()
         step()
     torch.cuda.synchronize()
-    eng.check()
+    for g in ins:
+        g["eng"].check()
 
     # --- timed region: K full insertions, L2 flushed between steps ----------
     if world > 1:
@@ -247,38 +258,46 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     t_steps = sum(s.elapsed_time(e) for s, e in ev) / 1e3  # s
-    eng.check()
+    for g in ins:
+        g["eng"].check()
 
     # --- dominant kernel: the contraction stage alone ------------------------
-    eng.run_stages(prob, N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
+    for g in ins:
+        g["eng"].run_stages(g["prob"], N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
     cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(3)]
-    for s, e in cev:
+    for s0, e0 in cev:
         flush.zero_()
-        s.record(stream)
-        eng.run_stages(prob, N.MG_STAGE_CONTRACT)
-        e.record(stream)
+        s0.record(stream)
+        for g in ins:
+            g["eng"].run_stages(g["prob"], N.MG_STAGE_CONTRACT)
+        e0.record(stream)
     torch.cuda.synchronize()
-    t_contract = float(np.mean([s.elapsed_time(e) for s, e in cev])) / 1e3
+    t_contract = float(np.mean([s0.elapsed_time(e0) for s0, e0 in cev])) / 1e3
 
     # --- end to end through the C ABI with host buffers -------------------------
-    host = {k: torch.from_numpy(np.ascontiguousarray(w[k], dtype=dt)).pin_memory()
-            for k, dt in (("x", np.float64), ("y", np.float64), ("sm_range", np.float64),
-                          ("h_eff", np.float32), ("v", np.float64), ("amp", np.float64))}
-    if w["kernel_index"] is not None:
-        host["kernel_index"] = torch.from_numpy(w["kernel_index"].astype(np.int8)).pin_memory()
-    if w["sigma"] is not None:
-        host["sigma"] = torch.from_numpy(w["sigma"].astype(np.float32)).pin_memory()
+    for g in ins:
+        s = g["s"]
+        host = {k: torch.from_numpy(np.ascontiguousarray(w[k][s], dtype=dt)).pin_memory()
+                for k, dt in (("x", np.float64), ("y", np.float64), ("sm_range", np.float64),
+                              ("h_eff", np.float32), ("v", np.float64), ("amp", np.float64))}
+        if w["kernel_index"] is not None:
+            host["kernel_index"] = torch.from_numpy(
+                w["kernel_index"][s].astype(np.int8)).pin_memory()
+        if w["sigma"] is not None:
+            host["sigma"] = torch.from_numpy(w["sigma"][s].astype(np.float32)).pin_memory()
+        g["host"] = host
+        g["dev"] = {k: getattr(g["parts"], k) for k in host}
     host_cube = torch.empty((nx, ny, nc), dtype=torch.float32).pin_memory()
     host_flux = torch.empty(nc + 1, dtype=torch.float64).pin_memory()
-    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    h2d = sum(t.numel() * t.element_size() for g in ins for t in g["host"].values())
     d2h = host_cube.numel() * 4 + host_flux.numel() * 8
-    dev_parts = {k: getattr(parts, k) for k in host}
 
     def e2e_step():
-        for k, t in host.items():
-            dev_parts[k].copy_(t, non_blocking=True)
-        eng.run(prob)
+        for g in ins:
+            for k, t in g["host"].items():
+                g["dev"][k].copy_(t, non_blocking=True)
+            g["eng"].run(g["prob"])
         host_cube.copy_(cube, non_blocking=True)
         host_flux.copy_(flux, non_blocking=True)
 
@@ -335,7 +354,8 @@ def main():
                    w["n_input"], "cube": [nx, ny, nc], "kernel": w["kernel_name"],
                    "spectrum": w["spectral_kind"], "form": a.form,
                    "l2": "flushed between steps (256 MiB write)", "parallelism":
-                   f"replicas{world}", "pairs": int(info.n_pairs), "items": int(info.n_items)},
+                   f"replicas{world}", "pairs": int(sum(g["info"].n_pairs for g in ins)),
+                   "groups": len(ins)},
         "particle_channel_updates_per_s": world * updates * a.steps / t_steps,
         "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf,
                      "unit": "TFLOP/s", "frac": achieved_tf / peak_tf, "traffic": traffic,
@@ -346,8 +366,8 @@ def main():
                      else "fallback 1.9 PFLOP/s"},
         "e2e": {"value": world / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": a.steps * launches_per_step(
-            a.form, w["spectral_model"] == N.MG_SPECTRUM_GAUSSIAN, nx, ny, nc),
+        "gpu_launches": a.steps * sum(launches_per_step(
+            a.form, g["prob"].spectral_model == N.MG_SPECTRUM_GAUSSIAN, nx, ny, nc) for g in ins),
         "step_ms": [round(s.elapsed_time(e), 3) for s, e in ev],
         "clocks": clk,
     }

@@ -99,6 +99,9 @@ typedef struct mg_problem {
   float* cube;                 /* [nx][ny][nc] output, Jy / pix^2, overwritten */
   double* flux;                /* optional [nc+1]: total flux (Jy), then per channel; NULL = skip */
   int32_t form;                /* MG_FORM_* */
+  int32_t accumulate;          /* 0: cube is overwritten; 1: the insertion is added to
+                                  the cube's contents (the reference's _array +=,
+                                  martini/martini.py:338); flux then sums the result */
 } mg_problem;
 
 /* sizes reported by mg_plan */

@@ -69,6 +69,7 @@ class Problem(C.Structure):
         ("padx", C.c_int32), ("pady", C.c_int32),
         ("edges", C.c_void_p), ("cube", C.c_void_p), ("flux", C.c_void_p),
         ("form", C.c_int32),
+        ("accumulate", C.c_int32),
     ]
 
 

@@ -194,6 +194,7 @@ int make_geo(const mg_problem* p, Geo* g) {
   g->spectral_model = p->spectral_model;
   g->sigma_const = p->sigma_const;
   g->form = p->form;
+  g->accumulate = p->accumulate != 0;
   for (int k = 0; k < p->n_kernels; ++k) {
     int t = p->kernels[k].type;
     if (t < MG_KERNEL_WENDLAND_C2 || t > MG_KERNEL_DIRAC)
@@ -306,7 +307,8 @@ int run(const mg_problem* p, void* ws, size_t bytes, cudaStream_t s, long long c
     launch_spec_store(g, w, p->n, num_sms(), s);
   cudaError_t e;
   if (stages & MG_STAGE_CONTRACT) {
-    e = cudaMemsetAsync(p->cube, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nc, s);
+    e = p->accumulate ? cudaSuccess
+                      : cudaMemsetAsync(p->cube, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nc, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(&w.hdr->item_counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return cuda_fail(e, "cube clear");
     if (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) {

@@ -147,7 +147,7 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
           const int c = it.c0 + tc * 4 + b;
-          if (c < g.nc) dst[c] = acc[a][b];
+          if (c < g.nc) dst[c] = g.accumulate ? dst[c] + acc[a][b] : acc[a][b];
         }
       }
     } else {
@@ -210,6 +210,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partials(Geo g, Ws w,
     const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
     if (i >= g.nx || j >= g.ny) continue;
     float* dst = cube + ((long long)i * g.ny + j) * g.nc + c;
+    if (g.accumulate) {
+      if (c < g.nc) acc.x += dst[0];
+      if (c + 1 < g.nc) acc.y += dst[1];
+      if (c + 2 < g.nc) acc.z += dst[2];
+      if (c + 3 < g.nc) acc.w += dst[3];
+    }
     if (c < g.nc) dst[0] = acc.x;
     if (c + 1 < g.nc) dst[1] = acc.y;
     if (c + 2 < g.nc) dst[2] = acc.z;

@@ -65,6 +65,7 @@ struct Geo {
   int spectral_model;
   float sigma_const;
   int form;
+  int accumulate;    // add into the cube instead of overwriting it
   KSpec ks[MG_MAX_KERNELS];
 };
 

@@ -851,17 +851,32 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
           }
         }
         if (inside || it.nk != 1) {
+          // cube writes add to the contents in accumulate mode (one writer
+          // per voxel: this item, or the split-K reduction)
+          const bool add = g.accumulate && it.nk == 1;
           if (vec && c + 32 <= limit) {
 #pragma unroll
-            for (int v = 0; v < 8; ++v)
-              *reinterpret_cast<float4*>(dst + c + 4 * v) = make_float4(
+            for (int v = 0; v < 8; ++v) {
+              float4 o = make_float4(
                   __uint_as_float(r[4 * v]) * unscale, __uint_as_float(r[4 * v + 1]) * unscale,
                   __uint_as_float(r[4 * v + 2]) * unscale,
                   __uint_as_float(r[4 * v + 3]) * unscale);
+              if (add) {
+                const float4 p4 = *reinterpret_cast<const float4*>(dst + c + 4 * v);
+                o.x += p4.x;
+                o.y += p4.y;
+                o.z += p4.z;
+                o.w += p4.w;
+              }
+              *reinterpret_cast<float4*>(dst + c + 4 * v) = o;
+            }
           } else {
 #pragma unroll
             for (int v = 0; v < 32; ++v)
-              if (c + v < limit) dst[c + v] = __uint_as_float(r[v]) * unscale;
+              if (c + v < limit) {
+                const float o = __uint_as_float(r[v]) * unscale;
+                dst[c + v] = add ? dst[c + v] + o : o;
+              }
           }
         }
       }

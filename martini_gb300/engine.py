@@ -73,7 +73,8 @@ class InsertionEngine:
     # ---- problem description ------------------------------------------------
     def problem(self, parts: DeviceParticles, kernels, spectral_model: int, sigma_const: float,
                 nx: int, ny: int, nc: int, padx: int, pady: int, edges: torch.Tensor,
-                cube: torch.Tensor, flux: torch.Tensor | None, form: int) -> N.Problem:
+                cube: torch.Tensor, flux: torch.Tensor | None, form: int,
+                accumulate: bool = False) -> N.Problem:
         p = N.Problem()
         p.n = parts.n
         p.x, p.y, p.sm_range = _ptr(parts.x), _ptr(parts.y), _ptr(parts.sm_range)
@@ -93,6 +94,7 @@ class InsertionEngine:
         p.cube = _ptr(cube)
         p.flux = _ptr(flux)
         p.form = int(form)
+        p.accumulate = int(bool(accumulate))
         return p
 
     def _workspace(self, nbytes: int) -> torch.Tensor:
@@ -137,17 +139,21 @@ class InsertionEngine:
     def insert(self, parts: DeviceParticles, kernels, spectral_model: int, sigma_const: float,
                nx: int, ny: int, nc: int, edges: torch.Tensor, padx: int = 0, pady: int = 0,
                form: int = N.MG_FORM_FP32, cube: torch.Tensor | None = None, flux: bool = True,
-               plan: bool = True, check: bool = True):
+               plan: bool = True, check: bool = True, accumulate: bool = False):
         """Insert particles into a (nx, ny, nc) float32 cube (Jy/pix^2).
 
         Returns (cube, flux) device tensors; flux[0] is the total flux in Jy
-        over the unpadded region and flux[1:] the per-channel sums.
+        over the unpadded region and flux[1:] the per-channel sums (of the
+        whole cube, so in accumulate mode including what it held before).
+        ``accumulate`` adds the insertion to ``cube`` instead of overwriting.
         """
+        if accumulate and cube is None:
+            raise ValueError("accumulate needs the cube to add into")
         if cube is None:
             cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=self.device)
         fl = torch.empty(nc + 1, dtype=torch.float64, device=self.device) if flux else None
         prob = self.problem(parts, kernels, spectral_model, sigma_const, nx, ny, nc, padx, pady,
-                            edges, cube, fl, form)
+                            edges, cube, fl, form, accumulate)
         if plan or self._ws is None:
             self.plan(prob)
         self.run(prob)

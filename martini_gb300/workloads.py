@@ -84,8 +84,9 @@ CONFIGS = {
                         kernel="WendlandC2Kernel", spectrum=("thermal", None),
                         disc=dict(R_d=10.0, h_med=0.5, h_dex=0.5)),
     "stress16m_2048": dict(n=16_000_000, seed=5, D=3.0, incl=60.0, nx=2048, nc=256, dv=4.0,
-                           px=10.0, kernel="WendlandC2Kernel", spectrum=("dirac", None),
-                           disc=dict(h_loguniform=(0.05, 20.0)), plummer=0.1),
+                           px=10.0, kernel="WendlandC2Kernel", spectrum=("thermal", None),
+                           disc=dict(h_loguniform=(0.05, 20.0)), plummer=0.1,
+                           dirac_fraction=0.2),
 }
 
 
@@ -127,14 +128,23 @@ def build(name: str, n: int | None = None):
     h_eff, kidx = kern._device_arrays()
     sigma, sig_const = sm._device_sigma(src)
     amp = src.mHI_g * np.power(src.skycoords.distance, -2.0) / MHI_TO_JY
+    # two spectral groups in one cube: a seeded subset with Dirac lines, the
+    # rest Gaussian (inserted by two calls, the second adding to the first)
+    groups = None
+    if cfg.get("dirac_fraction"):
+        pick = np.random.default_rng(cfg["seed"] + 1000).random(src.npart) < cfg["dirac_fraction"]
+        groups = [dict(sel=np.flatnonzero(~pick), spectral_model=sm.native_model),
+                  dict(sel=np.flatnonzero(pick), spectral_model=N.MG_SPECTRUM_DIRAC)]
     return dict(
+        groups=groups,
         name=name, n_input=n, n=src.npart, x=src.pixcoords[0], y=src.pixcoords[1],
         sm_range=kern.sm_ranges, h_eff=h_eff, kernel_index=kidx,
         v=src.skycoords.radial_velocity, sigma=sigma, sigma_const=sig_const, amp=amp,
         kernels=kern._device_kernels(), spectral_model=sm.native_model,
         edges=dc.velocity_channel_edges, nx=nx, ny=nx, nc=cfg["nc"], px_size=cfg["px"],
         distance=cfg["D"], mHI=src.mHI_g, dist=src.skycoords.distance,
-        spectral_kind=kind, kernel_name=cfg["kernel"], native_form_default=N.MG_FORM_FP32)
+        spectral_kind=kind if groups is None else f"{kind} + {cfg['dirac_fraction']:.0%} dirac",
+        kernel_name=cfg["kernel"], native_form_default=N.MG_FORM_FP32)
 
 
 def footprint_pixels(x, y, r, nx, ny):

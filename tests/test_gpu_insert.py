@@ -348,3 +348,46 @@ def test_wide_band(engine, form, nc):
                              c["h_eff"], spectra)
     got, flux = run_gpu(engine, c, form=form)
     assert_close(got, ref, flux, tol=FORM_TOL[form])
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+def test_accumulate_two_spectral_groups(engine, form):
+    """Two particle groups with different spectral models (Gaussian lines and
+    Dirac lines) inserted into one cube: the second call adds to the first
+    (accumulate mode, the reference's `_array +=`); the flux covers both.
+    Also checks that accumulate keeps what the cube held before."""
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles
+    rng = np.random.default_rng(41)
+    n, nx, ny, nc = 3000, 40, 36, 48
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    h = 10 ** rng.uniform(-0.3, 0.8, n)
+    kidx, size, resc = orc.select_kernels(kernels, h)
+    x, y = rng.normal(20, 7, n), rng.normal(18, 6, n)
+    ranges = orc.sm_ranges(h, size)
+    v, sig = rng.normal(250, 30, n), rng.uniform(4, 10, n)
+    mhi = 10 ** rng.uniform(4, 5, n)
+    amp = mhi / 9.0 / orc.MHI_TO_JY
+    edges = orc.vrad_channel_edges(nc, 4.0, 250.0)
+    dirac = rng.random(n) < 0.2
+    groups = [(~dirac, N.MG_SPECTRUM_GAUSSIAN, "gaussian"), (dirac, N.MG_SPECTRUM_DIRAC, "dirac")]
+    ref = np.zeros((nx, ny, nc))
+    for m, _, model in groups:
+        sp = orc.init_spectra(model, mhi[m], np.full(m.sum(), 3.0), v[m], edges,
+                              sig[m] if model == "gaussian" else None)
+        ref += orc.insert_scatter(nx, ny, x[m], y[m], ranges[m], kernels, kidx[m], (h * resc)[m],
+                                  sp)
+    base = np.linspace(0.0, 1e-3, nx * ny * nc).reshape(nx, ny, nc).astype(np.float32)
+    cube = torch.from_numpy(base).to(engine.device)
+    table = native_kernel_table(kernels)
+    e = torch.from_numpy(edges).to(engine.device)
+    for m, model, _ in groups:
+        parts = DeviceParticles.from_host(engine.device, x[m], y[m], ranges[m], (h * resc)[m],
+                                          kidx[m], v=v[m], sigma=sig[m], amp=amp[m])
+        _, flux = engine.insert(parts, table, model, 0.0, nx, ny, nc, e, form=form, cube=cube,
+                                accumulate=True)
+    got = cube.cpu().numpy().astype(np.float64) - base
+    peak = np.abs(ref).max()
+    assert np.abs(got - ref).max() / peak <= FORM_TOL[form]
+    tot = ref.sum() + base.astype(np.float64).sum()
+    assert abs(flux.cpu().numpy()[0] - tot) / tot <= TOL_FLUX
