@@ -173,6 +173,30 @@ int mg_insert_stages(const mg_problem* p, void* workspace, size_t workspace_byte
                      int64_t max_pairs, int64_t max_partial_items, int32_t stages, void* stream);
 
 /*
+ * Batches: several cubes in one insertion (a survey of many galaxies).  No
+ * counterpart in the reference, which inserts one source per Martini object
+ * (martini/martini.py:827-861); a population is a loop over Martini objects.
+ * Every problem of a batch must share the kernel table, spectral model,
+ * contraction form and accumulate flag; each has its own particles, cube,
+ * channel grid and flux.  One launch sequence bins all cubes together and
+ * one persistent contraction kernel works through all their tiles from a
+ * single queue, so small cubes do not pay a pipeline each.  The per-cube
+ * table is written to the workspace by kernels (no host copies), so a batch
+ * insertion can be captured in a CUDA graph.  Semantics otherwise as the
+ * single-problem calls (which are batches of one).  At most 65535 cubes.
+ */
+int mg_workspace_size_batched(const mg_problem* probs, int32_t nprob, int64_t max_pairs,
+                              int64_t max_partial_items, size_t* bytes);
+int mg_plan_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                    size_t workspace_bytes, void* stream, mg_plan_info* info);
+int mg_insert_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                      size_t workspace_bytes, int64_t max_pairs, int64_t max_partial_items,
+                      void* stream);
+int mg_insert_stages_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                             size_t workspace_bytes, int64_t max_pairs, int64_t max_partial_items,
+                             int32_t stages, void* stream);
+
+/*
  * Read back the device status word of the last mg_plan/mg_insert on this
  * workspace (SYNCHRONISES the stream).  Returns MG_OK, MG_ERR_WORKSPACE,
  * MG_ERR_NOT_MONOTONIC or MG_ERR_TIMEOUT.

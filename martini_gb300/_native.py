@@ -40,7 +40,9 @@ MG_MAX_KERNELS = 4
 
 # every symbol include/martini_gb300.h declares
 EXPORTS = ("mg_version", "mg_last_error", "mg_workspace_size", "mg_plan", "mg_insert",
-           "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux", "mg_insert_noalloc")
+           "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux", "mg_insert_noalloc",
+           "mg_workspace_size_batched", "mg_plan_batched", "mg_insert_batched",
+           "mg_insert_stages_batched")
 
 MG_NOALLOC_SCRATCH_BYTES = 128 << 20
 
@@ -109,6 +111,14 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.mg_insert_stages.argtypes = [P(Problem), C.c_void_p, C.c_size_t, C.c_int64, C.c_int64,
                                      C.c_int32, C.c_void_p]
     lib.mg_check.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mg_workspace_size_batched.argtypes = [P(Problem), C.c_int32, C.c_int64, C.c_int64,
+                                              P(C.c_size_t)]
+    lib.mg_plan_batched.argtypes = [P(Problem), C.c_int32, C.c_void_p, C.c_size_t, C.c_void_p,
+                                    P(PlanInfo)]
+    lib.mg_insert_batched.argtypes = [P(Problem), C.c_int32, C.c_void_p, C.c_size_t, C.c_int64,
+                                      C.c_int64, C.c_void_p]
+    lib.mg_insert_stages_batched.argtypes = [P(Problem), C.c_int32, C.c_void_p, C.c_size_t,
+                                             C.c_int64, C.c_int64, C.c_int32, C.c_void_p]
     lib.mg_insert_noalloc.argtypes = [P(Problem), C.c_void_p]
     lib.mg_spectra.argtypes = [P(Problem), C.c_void_p, C.c_void_p]
     lib.mg_flux.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

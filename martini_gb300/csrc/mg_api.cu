@@ -3,6 +3,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "mg_internal.cuh"
 
@@ -53,43 +54,47 @@ int channel_bits(int nc) {
 }
 
 struct Layout {
-  size_t hdr, rec, npairs, pair_off, tile_count, tile_diff, tile_wlo, tile_whi, tile_off, ehi, elo, inv_w,
-      keys, list, keys_tmp, list_tmp, rs_hist, rs_off, scan_sums, seg_lo, seg_hi, seg_items,
-      seg_part, item_off, part_off, partial, flux_part, total;
-  int nseg, ncb, width;
+  size_t hdr, gal, gst, gp0, gt0, gs0, ge0, gr0, rec, npairs, pair_off, tile_count, tile_diff,
+      tile_wlo, tile_whi, tile_off, ehi, elo, inv_w, keys, list, keys_tmp, list_tmp, rs_hist,
+      rs_off, scan_sums, seg_lo, seg_hi, seg_items, seg_part, item_off, part_off, partial,
+      flux_part, total;
 };
 
-Layout layout(long long n, int nx, int ny, int nc, int form, int flux_ch, long long cap_pairs,
-              long long cap_partial) {
+Layout layout(const Geo& g, long long cap_pairs, long long cap_partial) {
   Layout L;
-  const int ntx = (nx + TILE_I - 1) / TILE_I, nty = (ny + TILE_J - 1) / TILE_J;
-  const int ntiles = ntx * nty;
-  seg_shape(form, nc, &L.ncb, &L.width);
-  L.nseg = ntiles * L.ncb;
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = o;
     o += align256(bytes > 0 ? bytes : 1);
     return at;
   };
-  const size_t nn = (size_t)(n > 0 ? n : 1);
+  const size_t nn = (size_t)(g.n > 0 ? g.n : 1);
+  const size_t ng1 = (size_t)g.ngal + 1;
   const size_t cp = (size_t)(cap_pairs > 0 ? cap_pairs : 1);
   const long long rb = radix_blocks(cap_pairs > 0 ? cap_pairs : 1);
-  long long scan_n = n;
+  long long scan_n = g.n;
   if (256 * rb > scan_n) scan_n = 256 * rb;
-  if (L.nseg > scan_n) scan_n = L.nseg;
+  if (g.nseg > scan_n) scan_n = g.nseg;
+  if (g.ntiles > scan_n) scan_n = g.ntiles;
   L.hdr = take(sizeof(WsHeader));
+  L.gal = take(sizeof(Gal) * (size_t)g.ngal);
+  L.gst = take(sizeof(GalState) * (size_t)g.ngal);
+  L.gp0 = take(sizeof(long long) * ng1);
+  L.gt0 = take(sizeof(int) * ng1);
+  L.gs0 = take(sizeof(int) * ng1);
+  L.ge0 = take(sizeof(int) * ng1);
+  L.gr0 = take(sizeof(int) * ng1);
   L.rec = take(sizeof(PRec) * nn);
   L.npairs = take(sizeof(int) * nn);
   L.pair_off = take(sizeof(long long) * nn);
-  L.tile_count = take(sizeof(int) * ntiles);
-  L.tile_diff = take(sizeof(int) * (size_t)(ntx + 1) * (nty + 1));
-  L.tile_wlo = take(sizeof(int) * ntiles);
-  L.tile_whi = take(sizeof(int) * ntiles);
-  L.tile_off = take(sizeof(long long) * (ntiles + 1));
-  L.ehi = take(sizeof(float) * (nc + 1));
-  L.elo = take(sizeof(float) * (nc + 1));
-  L.inv_w = take(sizeof(float) * nc);
+  L.tile_count = take(sizeof(int) * (size_t)g.ntiles);
+  L.tile_diff = take(sizeof(int) * (size_t)g.ndiff);
+  L.tile_wlo = take(sizeof(int) * (size_t)g.ntiles);
+  L.tile_whi = take(sizeof(int) * (size_t)g.ntiles);
+  L.tile_off = take(sizeof(long long) * ((size_t)g.ntiles + 1));
+  L.ehi = take(sizeof(float) * (size_t)g.nedge);
+  L.elo = take(sizeof(float) * (size_t)g.nedge);
+  L.inv_w = take(sizeof(float) * (size_t)g.nedge);
   L.keys = take(sizeof(unsigned) * cp);
   L.list = take(sizeof(int) * cp);
   L.keys_tmp = take(sizeof(unsigned) * cp);
@@ -97,22 +102,30 @@ Layout layout(long long n, int nx, int ny, int nc, int form, int flux_ch, long l
   L.rs_hist = take(sizeof(int) * 256 * (size_t)rb);
   L.rs_off = take(sizeof(long long) * 256 * (size_t)rb);
   L.scan_sums = take(sizeof(long long) * (size_t)(scan_blocks(scan_n) + 1));
-  L.seg_lo = take(sizeof(long long) * L.nseg);
-  L.seg_hi = take(sizeof(long long) * L.nseg);
-  L.seg_items = take(sizeof(int) * L.nseg);
-  L.seg_part = take(sizeof(int) * L.nseg);
-  L.item_off = take(sizeof(long long) * L.nseg);
-  L.part_off = take(sizeof(long long) * L.nseg);
-  L.flux_part = take(sizeof(double) * (size_t)flux_ch * nc);
-  L.partial = take(sizeof(float) * (size_t)TILE_PX * L.width * (size_t)(cap_partial > 0 ? cap_partial : 0));
+  L.seg_lo = take(sizeof(long long) * (size_t)g.nseg);
+  L.seg_hi = take(sizeof(long long) * (size_t)g.nseg);
+  L.seg_items = take(sizeof(int) * (size_t)g.nseg);
+  L.seg_part = take(sizeof(int) * (size_t)g.nseg);
+  L.item_off = take(sizeof(long long) * (size_t)g.nseg);
+  L.part_off = take(sizeof(long long) * (size_t)g.nseg);
+  L.flux_part = take(sizeof(double) * (size_t)g.nfpart);
+  L.partial = take(sizeof(float) * (size_t)TILE_PX * g.max_width *
+                   (size_t)(cap_partial > 0 ? cap_partial : 0));
   L.total = o;
   return L;
 }
 
-Ws make_ws(void* base, const Layout& L, int nc) {
+Ws make_ws(void* base, const Layout& L) {
   char* b = static_cast<char*>(base);
   Ws w;
   w.hdr = reinterpret_cast<WsHeader*>(b + L.hdr);
+  w.gal = reinterpret_cast<Gal*>(b + L.gal);
+  w.gst = reinterpret_cast<GalState*>(b + L.gst);
+  w.gp0 = reinterpret_cast<long long*>(b + L.gp0);
+  w.gt0 = reinterpret_cast<int*>(b + L.gt0);
+  w.gs0 = reinterpret_cast<int*>(b + L.gs0);
+  w.ge0 = reinterpret_cast<int*>(b + L.ge0);
+  w.gr0 = reinterpret_cast<int*>(b + L.gr0);
   w.rec = reinterpret_cast<PRec*>(b + L.rec);
   w.npairs = reinterpret_cast<int*>(b + L.npairs);
   w.pair_off = reinterpret_cast<long long*>(b + L.pair_off);
@@ -139,10 +152,8 @@ Ws make_ws(void* base, const Layout& L, int nc) {
   w.part_off = reinterpret_cast<long long*>(b + L.part_off);
   w.partial = reinterpret_cast<float*>(b + L.partial);
   w.flux_part = reinterpret_cast<double*>(b + L.flux_part);
-  w.nseg = L.nseg;
-  w.ncb_seg = L.ncb;
-  w.seg_width = L.width;
-  w.cbits = channel_bits(nc);
+  w.spec = nullptr;
+  w.cap_spec = 0;
   return w;
 }
 
@@ -151,9 +162,9 @@ double gaussian_norm(double t) {
          2.0 * t / std::sqrt(2.0 * 3.14159265358979323846) * std::exp(-t * t / 2.0);
 }
 
-// Validate the problem and fill device-side geometry (no device access:
-// edge direction and monotonicity are resolved by the k_edges kernel).
-int make_geo(const mg_problem* p, Geo* g) {
+// Validate one problem (no device access: edge direction and monotonicity
+// are resolved by the k_edges kernel).
+int check_problem(const mg_problem* p) {
   if (!p) return fail(MG_ERR_INVALID_ARGUMENT, "null problem");
   if (p->nx <= 0 || p->ny <= 0 || p->nc <= 0)
     return fail(MG_ERR_INVALID_ARGUMENT, "cube dimensions must be positive");
@@ -179,37 +190,130 @@ int make_geo(const mg_problem* p, Geo* g) {
     return fail(MG_ERR_INVALID_ARGUMENT, "x, y, sm_range and h_eff are required");
   if (p->form != MG_FORM_FP32 && p->form != MG_FORM_BF16X3 && p->form != MG_FORM_F16X3)
     return fail(MG_ERR_INVALID_ARGUMENT, "unknown contraction form");
-  std::memset(g, 0, sizeof(Geo));
-  g->nx = p->nx;
-  g->ny = p->ny;
-  g->nc = p->nc;
-  g->padx = p->padx;
-  g->pady = p->pady;
-  g->ntx = (p->nx + TILE_I - 1) / TILE_I;
-  g->nty = (p->ny + TILE_J - 1) / TILE_J;
-  long long nt = (long long)g->ntx * g->nty;
-  if (nt > (1LL << 30)) return fail(MG_ERR_INVALID_ARGUMENT, "cube too large");
-  g->ntiles = (int)nt;
-  g->n_kernels = p->n_kernels;
-  g->spectral_model = p->spectral_model;
-  g->sigma_const = p->sigma_const;
-  g->form = p->form;
-  g->accumulate = p->accumulate != 0;
   for (int k = 0; k < p->n_kernels; ++k) {
-    int t = p->kernels[k].type;
+    const int t = p->kernels[k].type;
     if (t < MG_KERNEL_WENDLAND_C2 || t > MG_KERNEL_DIRAC)
       return fail(MG_ERR_INVALID_ARGUMENT, "unknown kernel type");
-    g->ks[k].type = t;
-    g->ks[k].truncate = p->kernels[k].truncate;
-    if (t == MG_KERNEL_GAUSSIAN) {
-      if (!(p->kernels[k].truncate >= 2.f))
-        return fail(MG_ERR_INVALID_ARGUMENT,
-                    "GaussianKernel with truncation <2sigma will cause large errors in total mass.");
-      g->ks[k].gnorm = (float)gaussian_norm(p->kernels[k].truncate);
-    } else {
-      g->ks[k].gnorm = 1.f;
-    }
+    if (t == MG_KERNEL_GAUSSIAN && !(p->kernels[k].truncate >= 2.f))
+      return fail(MG_ERR_INVALID_ARGUMENT,
+                  "GaussianKernel with truncation <2sigma will cause large errors in total mass.");
   }
+  return MG_OK;
+}
+
+// Host description of a batch: the per-cube table and the batch constants.
+struct Batch {
+  std::vector<Gal> gal;
+  Geo g;
+};
+
+// Validate a batch (every cube shares the kernel table, spectral model,
+// contraction form and accumulate flag) and lay its cubes out in the
+// batch-wide index spaces.  `shape_only` (workspace sizing) checks just
+// what the layout depends on: sizes, pads and form.
+int make_batch(const mg_problem* probs, int nprob, Batch* b, bool shape_only = false) {
+  if (!probs || nprob < 1) return fail(MG_ERR_INVALID_ARGUMENT, "empty batch");
+  if (nprob > 65535) return fail(MG_ERR_INVALID_ARGUMENT, "at most 65535 cubes in a batch");
+  for (int k = 0; k < nprob; ++k) {
+    const mg_problem& p = probs[k];
+    int rc = MG_OK;
+    if (!shape_only) {
+      rc = check_problem(&p);
+    } else if (p.nx <= 0 || p.ny <= 0 || p.nc <= 0 || p.n < 0) {
+      rc = fail(MG_ERR_INVALID_ARGUMENT, "invalid problem dimensions");
+    } else if (p.padx < 0 || p.pady < 0 || 2 * p.padx >= p.nx || 2 * p.pady >= p.ny) {
+      rc = fail(MG_ERR_INVALID_ARGUMENT, "invalid pad");
+    } else if (p.form != MG_FORM_FP32 && p.form != MG_FORM_BF16X3 && p.form != MG_FORM_F16X3) {
+      rc = fail(MG_ERR_INVALID_ARGUMENT, "unknown contraction form");
+    }
+    if (rc) return rc;
+  }
+  const mg_problem& p0 = probs[0];
+  for (int k = 1; k < nprob && !shape_only; ++k) {
+    const mg_problem& p = probs[k];
+    bool same = p.n_kernels == p0.n_kernels && p.spectral_model == p0.spectral_model &&
+                p.form == p0.form && (p.accumulate != 0) == (p0.accumulate != 0);
+    for (int j = 0; same && j < p0.n_kernels; ++j)
+      same = p.kernels[j].type == p0.kernels[j].type &&
+             p.kernels[j].truncate == p0.kernels[j].truncate;
+    if (!same)
+      return fail(MG_ERR_INVALID_ARGUMENT,
+                  "the problems of a batch must share kernels, spectral model, form and "
+                  "accumulate flag");
+  }
+  Geo& g = b->g;
+  std::memset(&g, 0, sizeof(Geo));
+  g.ngal = nprob;
+  g.n_kernels = p0.n_kernels;
+  g.spectral_model = p0.spectral_model;
+  g.form = p0.form;
+  g.accumulate = p0.accumulate != 0;
+  for (int k = 0; k < p0.n_kernels && k < MG_MAX_KERNELS; ++k) {
+    const int t = p0.kernels[k].type;
+    g.ks[k].type = t;
+    g.ks[k].truncate = p0.kernels[k].truncate;
+    g.ks[k].gnorm = t == MG_KERNEL_GAUSSIAN ? (float)gaussian_norm(p0.kernels[k].truncate) : 1.f;
+  }
+  b->gal.assign(nprob, Gal());
+  long long n = 0, ndiff = 0, nedge = 0, nfpart = 0, ntiles = 0, nseg = 0, nrows = 0;
+  for (int k = 0; k < nprob; ++k) {
+    const mg_problem& p = probs[k];
+    Gal& G = b->gal[k];
+    std::memset(&G, 0, sizeof(Gal));
+    G.x = p.x;
+    G.y = p.y;
+    G.r = p.sm_range;
+    G.h = p.h_eff;
+    G.kidx = p.kernel_index;
+    G.v = p.v;
+    G.sigma = p.sigma;
+    G.amp = p.amp;
+    G.spectra = p.spectra;
+    G.edges = p.edges;
+    G.cube = p.cube;
+    G.flux = p.flux;
+    G.sigma_const = p.sigma_const;
+    G.nx = p.nx;
+    G.ny = p.ny;
+    G.nc = p.nc;
+    G.padx = p.padx;
+    G.pady = p.pady;
+    G.ntx = (p.nx + TILE_I - 1) / TILE_I;
+    G.nty = (p.ny + TILE_J - 1) / TILE_J;
+    const long long nt = (long long)G.ntx * G.nty;
+    seg_shape(p.form, p.nc, &G.ncb, &G.width);
+    G.p0 = n;
+    G.n = p.n;
+    G.tile0 = (int)ntiles;
+    G.seg0 = (int)nseg;
+    G.diff0 = ndiff;
+    G.edge0 = (int)nedge;
+    G.row0 = (int)nrows;
+    G.fpart0 = nfpart;
+    G.ntiles = (int)nt;
+    const long long nd = (long long)(G.ntx + 1) * (G.nty + 1);
+    const int rows = p.nx - 2 * p.padx;
+    n += p.n;
+    ntiles += nt;
+    nseg += nt * G.ncb;
+    ndiff += nd;
+    nedge += p.nc + 1;
+    nrows += rows;
+    nfpart += (long long)rows * p.nc;
+    if (ntiles > (1LL << 30) || nseg > (1LL << 30) || nedge > (1LL << 30) || nrows > (1LL << 30))
+      return fail(MG_ERR_INVALID_ARGUMENT, "batch too large");
+    if (G.width > g.max_width) g.max_width = G.width;
+    if (p.nc > g.max_nc) g.max_nc = p.nc;
+    if (nd > g.max_diff) g.max_diff = nd > (1LL << 30) ? (1 << 30) : (int)nd;
+  }
+  g.n = n;
+  g.ntiles = (int)ntiles;
+  g.nseg = (int)nseg;
+  g.ndiff = ndiff;
+  g.nedge = nedge;
+  g.nrows = (int)nrows;
+  g.nfpart = nfpart;
+  g.cbits = channel_bits(g.max_nc);
   return MG_OK;
 }
 
@@ -224,42 +328,32 @@ int num_sms() {
   return sms;
 }
 
-PrepArgs prep_args(const mg_problem* p) {
-  PrepArgs a;
-  a.n = p->n;
-  a.x = p->x;
-  a.y = p->y;
-  a.r = p->sm_range;
-  a.h = p->h_eff;
-  a.kidx = p->kernel_index;
-  a.v = p->v;
-  a.sigma = p->sigma;
-  a.amp = p->amp;
-  a.edges = p->edges;
-  a.spectra = p->spectra;
-  return a;
-}
+bool tc_form(int form) { return form == MG_FORM_BF16X3 || form == MG_FORM_F16X3; }
 
-int workspace_view(const mg_problem* p, const Geo& g, void* ws, size_t bytes,
-                   long long cap_pairs, long long cap_partial, Ws* w) {
-  Layout L = layout(p->n, g.nx, g.ny, g.nc, p->form, flux_chunks(g.nx, g.padx), cap_pairs,
-                    cap_partial);
+int workspace_view(const Geo& g, void* ws, size_t bytes, long long cap_pairs,
+                   long long cap_partial, Ws* w) {
+  Layout L = layout(g, cap_pairs, cap_partial);
   if (!ws || bytes < L.total)
     return fail(MG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(L.total) +
                                       " bytes, have " + std::to_string(bytes));
-  *w = make_ws(ws, L, g.nc);
+  *w = make_ws(ws, L);
+  if (sort_bits(g) > 32) return fail(MG_ERR_INVALID_ARGUMENT, "cube too large for the sort key");
   // the workspace beyond the fixed layout holds the spectrum store of the
   // tensor-core forms (Gaussian lines); without room they evaluate in-kernel
-  if ((p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) &&
-      p->spectral_model == MG_SPECTRUM_GAUSSIAN) {
+  if (tc_form(g.form) && g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
     w->spec = reinterpret_cast<float*>(static_cast<char*>(ws) + L.total);
     w->cap_spec = (long long)((bytes - L.total) / sizeof(float));
-  } else {
-    w->spec = nullptr;
-    w->cap_spec = 0;
   }
-  if (sort_bits(g, *w) > 32) return fail(MG_ERR_INVALID_ARGUMENT, "cube too large for the sort key");
   return MG_OK;
+}
+
+// Zero the cubes of a batch (one block row per cube).
+__global__ void k_clear_cubes(Geo g, Ws w) {
+  const Gal& G = w.gal[blockIdx.y];
+  const long long n = (long long)G.nx * G.ny * G.nc;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x)
+    G.cube[k] = 0.f;
 }
 
 }  // namespace
@@ -268,20 +362,28 @@ void mg::set_last_error(const std::string& msg) { g_err = msg; }
 
 extern "C" {
 
-const char* mg_version(void) { return "martini_gb300 0.1 (sm_103a)"; }
+const char* mg_version(void) { return "martini_gb300 0.2 (sm_103a)"; }
 
 const char* mg_last_error(void) { return g_err.c_str(); }
+
+int mg_workspace_size_batched(const mg_problem* probs, int32_t nprob, int64_t max_pairs,
+                              int64_t max_partial_items, size_t* bytes) {
+  if (!probs || !bytes) return fail(MG_ERR_INVALID_ARGUMENT, "null argument");
+  if (max_pairs < 0 || max_partial_items < 0)
+    return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
+  Batch b;
+  int rc = make_batch(probs, nprob, &b, true);
+  if (rc) return rc;
+  *bytes = layout(b.g, max_pairs, max_partial_items).total;
+  return MG_OK;
+}
 
 int mg_workspace_size(const mg_problem* p, int64_t max_pairs, int64_t max_partial_items,
                       size_t* bytes) {
   if (!p || !bytes) return fail(MG_ERR_INVALID_ARGUMENT, "null argument");
   if (p->nx <= 0 || p->ny <= 0 || p->nc <= 0 || p->n < 0)
     return fail(MG_ERR_INVALID_ARGUMENT, "invalid problem dimensions");
-  if (max_pairs < 0 || max_partial_items < 0)
-    return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
-  *bytes = layout(p->n, p->nx, p->ny, p->nc, p->form, flux_chunks(p->nx, p->padx), max_pairs,
-                  max_partial_items).total;
-  return MG_OK;
+  return mg_workspace_size_batched(p, 1, max_pairs, max_partial_items, bytes);
 }
 
 }  // extern "C"
@@ -290,41 +392,52 @@ namespace {
 
 // The stages of an insertion (MG_STAGE_* bits; `scatter` adds the particle
 // list to the binning stage); all asynchronous on stream s.
-int run(const mg_problem* p, void* ws, size_t bytes, cudaStream_t s, long long cap_pairs,
-        long long cap_partial, int stages, bool scatter, Ws* wout, Geo* gout) {
-  Geo g;
-  int rc = make_geo(p, &g);
+int run(const mg_problem* probs, int nprob, void* ws, size_t bytes, cudaStream_t s,
+        long long cap_pairs, long long cap_partial, int stages, bool scatter, Ws* wout,
+        Batch* bout) {
+  Batch& b = *bout;
+  int rc = make_batch(probs, nprob, &b);
   if (rc) return rc;
+  const Geo& g = b.g;
   if (cap_pairs < 0 || cap_partial < 0) return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
   Ws w;
-  rc = workspace_view(p, g, ws, bytes, cap_pairs, cap_partial, &w);
+  rc = workspace_view(g, ws, bytes, cap_pairs, cap_partial, &w);
   if (rc) return rc;
+  launch_set_gals(b.gal.data(), g, w, s);
   if (stages & MG_STAGE_BIN) {
-    launch_prep(prep_args(p), g, w, num_sms(), s, cap_pairs, cap_partial);
-    if (scatter) launch_sort_segments(prep_args(p), g, w, cap_pairs, num_sms(), s);
+    launch_prep(g, w, num_sms(), s, cap_pairs, cap_partial);
+    if (scatter) launch_sort_segments(g, w, cap_pairs, num_sms(), s);
   }
-  if ((stages & MG_STAGE_SPEC) && (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3))
-    launch_spec_store(g, w, p->n, num_sms(), s);
+  if ((stages & MG_STAGE_SPEC) && tc_form(g.form)) launch_spec_store(g, w, num_sms(), s);
   cudaError_t e;
   if (stages & MG_STAGE_CONTRACT) {
-    e = p->accumulate ? cudaSuccess
-                      : cudaMemsetAsync(p->cube, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nc, s);
+    e = cudaSuccess;
+    if (!g.accumulate) {
+      if (g.ngal == 1) {
+        const Gal& G = b.gal[0];
+        e = cudaMemsetAsync(G.cube, 0, sizeof(float) * (size_t)G.nx * G.ny * G.nc, s);
+      } else {
+        k_clear_cubes<<<dim3(64, (unsigned)g.ngal), 256, 0, s>>>(g, w);
+      }
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(&w.hdr->item_counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return cuda_fail(e, "cube clear");
-    if (p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) {
-      rc = launch_contract_bf16x3(g, w, p->spectra, p->cube, num_sms(), s);
+    if (tc_form(g.form)) {
+      rc = launch_contract_bf16x3(g, w, num_sms(), s);
       if (rc == MG_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tensor-core kernel set-up");
       if (rc) return fail(rc, "tensor-core form does not support this cube (band too wide)");
     } else {
-      launch_contract_fp32(g, w, p->spectra, p->cube, num_sms(), s);
+      launch_contract_fp32(g, w, num_sms(), s);
     }
   }
-  if ((stages & MG_STAGE_FLUX) && p->flux)
-    launch_flux(p->cube, p->nx, p->ny, p->nc, p->padx, p->pady, w.flux_part, p->flux, s);
+  if (stages & MG_STAGE_FLUX) {
+    bool any = false;
+    for (const Gal& G : b.gal) any = any || G.flux != nullptr;
+    if (any) launch_flux_batch(g, w, s);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   *wout = w;
-  *gout = g;
   return MG_OK;
 }
 
@@ -332,13 +445,13 @@ int run(const mg_problem* p, void* ws, size_t bytes, cudaStream_t s, long long c
 
 extern "C" {
 
-int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* stream,
-            mg_plan_info* info) {
+int mg_plan_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                    size_t workspace_bytes, void* stream, mg_plan_info* info) {
   if (!info) return fail(MG_ERR_INVALID_ARGUMENT, "null info");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   Ws w;
-  Geo g;
-  int rc = run(p, workspace, workspace_bytes, s, 0, 0, MG_STAGE_BIN, false, &w, &g);
+  Batch b;
+  int rc = run(probs, nprob, workspace, workspace_bytes, s, 0, 0, MG_STAGE_BIN, false, &w, &b);
   if (rc) return rc;
   WsHeader h;
   cudaError_t e = cudaMemcpyAsync(&h, w.hdr, sizeof(h), cudaMemcpyDeviceToHost, s);
@@ -348,34 +461,46 @@ int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* 
   info->n_pairs = h.n_pairs;
   info->n_items = 0;
   info->n_partial_items = h.partial_bound;
-  info->n_tiles = g.ntiles;
+  info->n_tiles = b.g.ntiles;
   size_t spec_bytes = 0;
-  if ((p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3) &&
-      p->spectral_model == MG_SPECTRUM_GAUSSIAN)
+  if (tc_form(b.g.form) && b.g.spectral_model == MG_SPECTRUM_GAUSSIAN)
     spec_bytes = align256(sizeof(float) * (size_t)h.spec_bound);
-  info->workspace_bytes = layout(p->n, g.nx, g.ny, g.nc, p->form, flux_chunks(g.nx, g.padx),
-                                 h.n_pairs, h.partial_bound).total +
-                          spec_bytes;
+  info->workspace_bytes = layout(b.g, h.n_pairs, h.partial_bound).total + spec_bytes;
   return MG_OK;
 }
 
-}  // extern "C"
+int mg_plan(const mg_problem* p, void* workspace, size_t workspace_bytes, void* stream,
+            mg_plan_info* info) {
+  return mg_plan_batched(p, 1, workspace, workspace_bytes, stream, info);
+}
 
-extern "C" {
+int mg_insert_stages_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                             size_t workspace_bytes, int64_t max_pairs, int64_t max_partial_items,
+                             int32_t stages, void* stream) {
+  if (stages & ~MG_STAGE_ALL) return fail(MG_ERR_INVALID_ARGUMENT, "unknown stage bits");
+  Ws w;
+  Batch b;
+  return run(probs, nprob, workspace, workspace_bytes, static_cast<cudaStream_t>(stream),
+             max_pairs, max_partial_items, stages, true, &w, &b);
+}
+
+int mg_insert_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                      size_t workspace_bytes, int64_t max_pairs, int64_t max_partial_items,
+                      void* stream) {
+  return mg_insert_stages_batched(probs, nprob, workspace, workspace_bytes, max_pairs,
+                                  max_partial_items, MG_STAGE_ALL, stream);
+}
 
 int mg_insert(const mg_problem* p, void* workspace, size_t workspace_bytes, int64_t max_pairs,
               int64_t max_partial_items, void* stream) {
-  return mg_insert_stages(p, workspace, workspace_bytes, max_pairs, max_partial_items,
-                          MG_STAGE_ALL, stream);
+  return mg_insert_stages_batched(p, 1, workspace, workspace_bytes, max_pairs, max_partial_items,
+                                  MG_STAGE_ALL, stream);
 }
 
 int mg_insert_stages(const mg_problem* p, void* workspace, size_t workspace_bytes,
                      int64_t max_pairs, int64_t max_partial_items, int32_t stages, void* stream) {
-  if (stages & ~MG_STAGE_ALL) return fail(MG_ERR_INVALID_ARGUMENT, "unknown stage bits");
-  Ws w;
-  Geo g;
-  return run(p, workspace, workspace_bytes, static_cast<cudaStream_t>(stream), max_pairs,
-             max_partial_items, stages, true, &w, &g);
+  return mg_insert_stages_batched(p, 1, workspace, workspace_bytes, max_pairs, max_partial_items,
+                                  stages, stream);
 }
 
 int mg_check(void* workspace, void* stream) {

@@ -75,305 +75,363 @@ __device__ __forceinline__ void channel_range(const double* e, int nc, int dec, 
 }
 
 
-// One thread per particle: exact footprint, Dirac pixel, spectral support,
-// packed record.  Tile coverage goes into a 2D difference array over the
-// tile grid, (ntx + 1) x (nty + 1): +1 at the corners (tx0, ty0) and
-// (tx1 + 1, ty1 + 1), -1 at (tx0, ty1 + 1) and (tx1 + 1, ty0), so four
-// integer atomics per particle whatever its footprint; k_plan_tiles turns
-// it into exact per-tile counts with prefix sums.  The array lives in
-// shared memory when it fits (PREP_SMEM_DIFF) and is flushed once per block.
-// The per-tile channel windows (needed only when a tile has several channel
-// blocks) and the header maxima are reduced per block before their global
-// atomics.
+// ---------------------------------------------------------------------------
+// The galaxy table: kernel parameters into the workspace (no host copy, so
+// the insertion can be captured in a CUDA graph).
+// ---------------------------------------------------------------------------
+
+constexpr int GALS_PER_SET = 16;
+struct GalChunk {
+  Gal g[GALS_PER_SET];
+};
+static_assert(sizeof(GalChunk) <= 3584, "galaxy chunk must fit the 4 KB parameter space");
+
+__global__ void k_set_gals(GalChunk c, int first, int count, Geo g, Ws w) {
+  const int k = threadIdx.x;
+  if (k < count) {
+    const Gal& G = c.g[k];
+    const int gi = first + k;
+    w.gal[gi] = G;
+    w.gp0[gi] = G.p0;
+    w.gt0[gi] = G.tile0;
+    w.gs0[gi] = G.seg0;
+    w.ge0[gi] = G.edge0;
+    w.gr0[gi] = G.row0;
+  }
+  if (k == 0 && first + count == g.ngal) {
+    w.gp0[g.ngal] = g.n;
+    w.gt0[g.ngal] = g.ntiles;
+    w.gs0[g.ngal] = g.nseg;
+    w.ge0[g.ngal] = (int)g.nedge;
+    w.gr0[g.ngal] = g.nrows;
+  }
+}
+
+void launch_set_gals(const Gal* gals, const Geo& g, const Ws& w, cudaStream_t s) {
+  for (int first = 0; first < g.ngal; first += GALS_PER_SET) {
+    GalChunk c;
+    const int count = g.ngal - first < GALS_PER_SET ? g.ngal - first : GALS_PER_SET;
+    for (int k = 0; k < count; ++k) c.g[k] = gals[first + k];
+    k_set_gals<<<1, 32, 0, s>>>(c, first, count, g, w);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Records and tile coverage
+// ---------------------------------------------------------------------------
+
+// One thread per particle of the batch: exact footprint, Dirac pixel,
+// spectral support, packed record.  Tile coverage goes into the cube's 2D
+// difference array over its tile grid, (ntx + 1) x (nty + 1): +1 at the
+// corners (tx0, ty0) and (tx1 + 1, ty1 + 1), -1 at (tx0, ty1 + 1) and
+// (tx1 + 1, ty0), so four integer atomics per particle whatever its
+// footprint; k_diff_prefix turns them into exact per-tile counts.  For a
+// single cube whose array fits (PREP_SMEM_DIFF) the array lives in shared
+// memory and is flushed once per block.  The per-tile channel windows (needed
+// only when a tile has several channel blocks) use global atomics; the
+// per-cube maxima are reduced over the warp when its particles share a cube.
 constexpr int PREP_THREADS = 256;
 constexpr int PREP_SMEM_DIFF = 12288;
 
-__global__ void __launch_bounds__(PREP_THREADS) k_prep(PrepArgs a, Geo g, Ws w) {
-  extern __shared__ int s_diff[];  // the difference array when it fits
-  __shared__ int s_wmax;
-  __shared__ unsigned s_wb, s_sb;
+__global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
+  extern __shared__ int s_diff[];  // the difference array of a single cube when it fits
   __shared__ unsigned long long s_spec;
-  const int dw = g.nty + 1;
-  const int ndiff = (g.ntx + 1) * dw;
-  const bool smem_hist = ndiff <= PREP_SMEM_DIFF;
-  int* const diff = smem_hist ? s_diff : w.tile_diff;
-  const bool windows = w.ncb_seg > 1;
+  const bool smem_hist = g.ngal == 1 && g.ndiff <= PREP_SMEM_DIFF;
   if (smem_hist)
-    for (int t = threadIdx.x; t < ndiff; t += blockDim.x) s_diff[t] = 0;
-  if (threadIdx.x == 0) {
-    s_wmax = 0;
-    s_wb = s_sb = 0u;
-    s_spec = 0ull;
-  }
+    for (int t = threadIdx.x; t < (int)g.ndiff; t += blockDim.x) s_diff[t] = 0;
+  if (threadIdx.x == 0) s_spec = 0ull;
   __syncthreads();
-  const int dec = w.hdr->edges_dec;
-  int my_wmax = 0;
-  unsigned my_wb = 0u, my_sb = 0u;
   unsigned my_spec = 0u;  // support channels of this thread's particles
+  const int lane = threadIdx.x & 31;
   // every thread of a block runs the same number of iterations
-  for (long long base = blockIdx.x * (long long)blockDim.x; base < a.n;
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < g.n;
        base += (long long)gridDim.x * blockDim.x) {
-    const long long p = base + threadIdx.x;
-    if (p >= a.n) continue;
-    PRec rec;
-    rec.ilo = 0; rec.ihi = -1; rec.jlo = 0; rec.jhi = -1;
-    rec.clo = 1; rec.chi = 0;
-    rec.xi = rec.yi = 0;
-    rec.xf = rec.yf = 0.f;
-    rec.h = 1.f; rec.inv_h2 = 1.f;
-    rec.vhi = rec.vlo = 0.f; rec.inv_s = 0.f; rec.amp = 0.f; rec.pad_ = 0;
-    int ks = a.kidx ? (int)a.kidx[p] : 0;
-    if (ks < 0 || ks >= g.n_kernels) ks = 0;  // -1: kernels[0] (sph_kernels.py:1360)
-    rec.kslot = ks;
-    double x = a.x[p], y = a.y[p], r = a.r[p];
-    // |coordinate| > 2^30 px cannot reach the cube (and would overflow int)
-    bool ok = isfinite(x) && isfinite(y) && fabs(x) < 1073741824.0 && fabs(y) < 1073741824.0;
-    if (ok) {
-      box_bounds(x, r, g.nx, rec.ilo, rec.ihi);
-      box_bounds(y, r, g.ny, rec.jlo, rec.jhi);
-      ok = rec.ilo <= rec.ihi && rec.jlo <= rec.jhi;
-    }
-    if (ok && g.ks[ks].type == MG_KERNEL_DIRAC) {
-      // weight 1 iff |x - i| < 0.5 and |y - j| < 0.5 (sph_kernels.py:1165):
-      // at most one pixel per axis, tested in FP64.
-      int di = -1, dj = -1;
-      double fx = floor(x), fy = floor(y);
-      if (fabs(x - fx) < 0.5) di = (int)fx; else if (fabs(x - (fx + 1.0)) < 0.5) di = (int)fx + 1;
-      if (fabs(y - fy) < 0.5) dj = (int)fy; else if (fabs(y - (fy + 1.0)) < 0.5) dj = (int)fy + 1;
-      if (di < rec.ilo || di > rec.ihi || dj < rec.jlo || dj > rec.jhi) {
-        ok = false;
-      } else {
-        rec.ilo = rec.ihi = di;
-        rec.jlo = rec.jhi = dj;
-      }
-    }
-    if (ok) {
-      double fx = floor(x), fy = floor(y);
-      rec.xi = (int)fx;
-      rec.yi = (int)fy;
-      rec.xf = (float)(x - fx);
-      rec.yf = (float)(y - fy);
-      float h = a.h ? a.h[p] : 1.f;
-      rec.h = h;
-      rec.inv_h2 = 1.f / (h * h);
-      if (g.spectral_model == MG_SPECTRUM_TABLE) {
-        rec.clo = 0;
-        rec.chi = g.nc - 1;
-        rec.amp = 1.f;
-      } else {
-        double v = a.v[p];
-        double am = a.amp[p];
-        rec.amp = (float)am;
-        double vh = (double)(float)v;
-        rec.vhi = (float)vh;
-        rec.vlo = (float)(v - vh);
-        if (g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
-          double s = a.sigma ? (double)a.sigma[p] : (double)g.sigma_const;
-          rec.inv_s = (float)(1.0 / (1.4142135623730951 * s));
-          // |u| <= 4.5: beyond it each wing holds erfc(4.5) / 2 = 1e-10 of
-          // the line's flux
-          double half = 4.5 * 1.4142135623730951 * s;
-          channel_range(a.edges, g.nc, dec, v - half, v + half, rec.clo, rec.chi);
-        } else {
-          channel_range(a.edges, g.nc, dec, v, v, rec.clo, rec.chi);
-        }
-        if (am == 0.0 || !isfinite(v)) {
-          rec.clo = 1;
-          rec.chi = 0;
-        }
-      }
-      ok = rec.clo <= rec.chi;
-    }
-    if (!ok) {
+    const long long P = base + threadIdx.x;
+    const bool valid = P < g.n;
+    const int gk = valid ? find_gal(w.gp0, g.ngal, P) : 0;
+    const Gal& G = w.gal[gk];
+    int wmax_v = 0;
+    unsigned wb_v = 0u, sb_v = 0u;
+    if (valid) {
+      const long long p = P - G.p0;
+      const int dec = w.gst[gk].dec;
+      const double* edges = G.edges;
+      PRec rec;
       rec.ilo = 0; rec.ihi = -1; rec.jlo = 0; rec.jhi = -1;
-    }
-    w.rec[p] = rec;
-    int np = 0;
-    if (ok) {
-      int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
-      int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
-      np = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
-      atomicAdd(&diff[tx0 * dw + ty0], 1);
-      atomicAdd(&diff[tx0 * dw + ty1 + 1], -1);
-      atomicAdd(&diff[(tx1 + 1) * dw + ty0], -1);
-      atomicAdd(&diff[(tx1 + 1) * dw + ty1 + 1], 1);
-      if (windows)
-        for (int tx = tx0; tx <= tx1; ++tx)
-          for (int ty = ty0; ty <= ty1; ++ty) {
-            const int t = tx * g.nty + ty;
-            atomicMin(&w.tile_wlo[t], rec.clo);
-            atomicMax(&w.tile_whi[t], rec.chi);
-          }
-      my_wmax = max(my_wmax, rec.chi - rec.clo);
-      my_spec += (unsigned)(rec.chi - rec.clo + 1);
-      if (g.form == MG_FORM_F16X3) {
-        // magnitude bounds for the scaled FP16 split (non-negative floats
-        // order like their bit patterns)
-        const KSpec k = g.ks[ks];
-        float wb = weight_bound(k.type, rec.inv_h2, k.gnorm);
-        my_wb = max(my_wb, __float_as_uint(wb));
-        float sb = rec.amp;
-        if (g.spectral_model == MG_SPECTRUM_TABLE) {
-          sb = 0.f;
-          for (int c = 0; c < g.nc; ++c) sb = fmaxf(sb, fabsf(a.spectra[p * g.nc + c]));
-        }
-        my_sb = max(my_sb, __float_as_uint(sb));
+      rec.clo = 1; rec.chi = 0;
+      rec.xi = rec.yi = 0;
+      rec.xf = rec.yf = 0.f;
+      rec.h = 1.f; rec.inv_h2 = 1.f;
+      rec.vhi = rec.vlo = 0.f; rec.inv_s = 0.f; rec.amp = 0.f; rec.pad_ = 0;
+      int ks = G.kidx ? (int)G.kidx[p] : 0;
+      if (ks < 0 || ks >= g.n_kernels) ks = 0;  // -1: kernels[0] (sph_kernels.py:1360)
+      rec.kslot = ks;
+      double x = G.x[p], y = G.y[p], r = G.r[p];
+      // |coordinate| > 2^30 px cannot reach the cube (and would overflow int)
+      bool ok = isfinite(x) && isfinite(y) && fabs(x) < 1073741824.0 && fabs(y) < 1073741824.0;
+      if (ok) {
+        box_bounds(x, r, G.nx, rec.ilo, rec.ihi);
+        box_bounds(y, r, G.ny, rec.jlo, rec.jhi);
+        ok = rec.ilo <= rec.ihi && rec.jlo <= rec.jhi;
       }
+      if (ok && g.ks[ks].type == MG_KERNEL_DIRAC) {
+        // weight 1 iff |x - i| < 0.5 and |y - j| < 0.5 (sph_kernels.py:1165):
+        // at most one pixel per axis, tested in FP64.
+        int di = -1, dj = -1;
+        double fx = floor(x), fy = floor(y);
+        if (fabs(x - fx) < 0.5) di = (int)fx; else if (fabs(x - (fx + 1.0)) < 0.5) di = (int)fx + 1;
+        if (fabs(y - fy) < 0.5) dj = (int)fy; else if (fabs(y - (fy + 1.0)) < 0.5) dj = (int)fy + 1;
+        if (di < rec.ilo || di > rec.ihi || dj < rec.jlo || dj > rec.jhi) {
+          ok = false;
+        } else {
+          rec.ilo = rec.ihi = di;
+          rec.jlo = rec.jhi = dj;
+        }
+      }
+      if (ok) {
+        double fx = floor(x), fy = floor(y);
+        rec.xi = (int)fx;
+        rec.yi = (int)fy;
+        rec.xf = (float)(x - fx);
+        rec.yf = (float)(y - fy);
+        float h = G.h ? G.h[p] : 1.f;
+        rec.h = h;
+        rec.inv_h2 = 1.f / (h * h);
+        if (g.spectral_model == MG_SPECTRUM_TABLE) {
+          rec.clo = 0;
+          rec.chi = G.nc - 1;
+          rec.amp = 1.f;
+        } else {
+          double v = G.v[p];
+          double am = G.amp[p];
+          rec.amp = (float)am;
+          double vh = (double)(float)v;
+          rec.vhi = (float)vh;
+          rec.vlo = (float)(v - vh);
+          if (g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
+            double sg = G.sigma ? (double)G.sigma[p] : (double)G.sigma_const;
+            rec.inv_s = (float)(1.0 / (1.4142135623730951 * sg));
+            // |u| <= 4.5: beyond it each wing holds erfc(4.5) / 2 = 1e-10 of
+            // the line's flux
+            double half = 4.5 * 1.4142135623730951 * sg;
+            channel_range(edges, G.nc, dec, v - half, v + half, rec.clo, rec.chi);
+          } else {
+            channel_range(edges, G.nc, dec, v, v, rec.clo, rec.chi);
+          }
+          if (am == 0.0 || !isfinite(v)) {
+            rec.clo = 1;
+            rec.chi = 0;
+          }
+        }
+        ok = rec.clo <= rec.chi;
+      }
+      if (!ok) {
+        rec.ilo = 0; rec.ihi = -1; rec.jlo = 0; rec.jhi = -1;
+      }
+      w.rec[P] = rec;
+      int np = 0;
+      if (ok) {
+        const int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
+        const int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
+        np = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+        const int dw = G.nty + 1;
+        int* const diff = smem_hist ? s_diff : w.tile_diff + G.diff0;
+        atomicAdd(&diff[tx0 * dw + ty0], 1);
+        atomicAdd(&diff[tx0 * dw + ty1 + 1], -1);
+        atomicAdd(&diff[(tx1 + 1) * dw + ty0], -1);
+        atomicAdd(&diff[(tx1 + 1) * dw + ty1 + 1], 1);
+        if (G.ncb > 1)
+          for (int tx = tx0; tx <= tx1; ++tx)
+            for (int ty = ty0; ty <= ty1; ++ty) {
+              const int t = G.tile0 + tx * G.nty + ty;
+              atomicMin(&w.tile_wlo[t], rec.clo);
+              atomicMax(&w.tile_whi[t], rec.chi);
+            }
+        wmax_v = rec.chi - rec.clo;
+        my_spec += (unsigned)(rec.chi - rec.clo + 1);
+        if (g.form == MG_FORM_F16X3) {
+          // magnitude bounds for the scaled FP16 split (non-negative floats
+          // order like their bit patterns)
+          const KSpec k = g.ks[ks];
+          wb_v = __float_as_uint(weight_bound(k.type, rec.inv_h2, k.gnorm));
+          float sb = rec.amp;
+          if (g.spectral_model == MG_SPECTRUM_TABLE) {
+            sb = 0.f;
+            for (int c = 0; c < G.nc; ++c) sb = fmaxf(sb, fabsf(G.spectra[p * G.nc + c]));
+          }
+          sb_v = __float_as_uint(sb);
+        }
+      }
+      w.npairs[P] = np;
     }
-    w.npairs[p] = np;
+    // per-cube maxima: one atomic per warp when its particles share a cube
+    const int g0 = __shfl_sync(0xffffffffu, gk, 0);
+    if (__all_sync(0xffffffffu, gk == g0)) {
+      wmax_v = __reduce_max_sync(0xffffffffu, wmax_v);
+      wb_v = __reduce_max_sync(0xffffffffu, wb_v);
+      sb_v = __reduce_max_sync(0xffffffffu, sb_v);
+      if (lane == 0) {
+        if (wmax_v) atomicMax(&w.gst[g0].wmax, wmax_v);
+        if (wb_v) atomicMax(&w.gst[g0].wbound_bits, wb_v);
+        if (sb_v) atomicMax(&w.gst[g0].sbound_bits, sb_v);
+      }
+    } else if (valid) {
+      if (wmax_v) atomicMax(&w.gst[gk].wmax, wmax_v);
+      if (wb_v) atomicMax(&w.gst[gk].wbound_bits, wb_v);
+      if (sb_v) atomicMax(&w.gst[gk].sbound_bits, sb_v);
+    }
   }
-  my_wmax = __reduce_max_sync(0xffffffffu, my_wmax);
-  my_wb = __reduce_max_sync(0xffffffffu, my_wb);
-  my_sb = __reduce_max_sync(0xffffffffu, my_sb);
   my_spec = __reduce_add_sync(0xffffffffu, my_spec);
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&s_wmax, my_wmax);
-    atomicMax(&s_wb, my_wb);
-    atomicMax(&s_sb, my_sb);
-    atomicAdd(&s_spec, (unsigned long long)my_spec);
-  }
+  if (lane == 0) atomicAdd(&s_spec, (unsigned long long)my_spec);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    atomicMax(&w.hdr->wmax, s_wmax);
-    if (g.spectral_model == MG_SPECTRUM_GAUSSIAN)
-      atomicAdd(reinterpret_cast<unsigned long long*>(&w.hdr->spec_bound), s_spec);
-    if (g.form == MG_FORM_F16X3) {
-      atomicMax(&w.hdr->wbound_bits, s_wb);
-      atomicMax(&w.hdr->sbound_bits, s_sb);
-    }
-  }
+  if (threadIdx.x == 0 && g.spectral_model == MG_SPECTRUM_GAUSSIAN)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&w.hdr->spec_bound), s_spec);
   if (smem_hist)
-    for (int t = threadIdx.x; t < ndiff; t += blockDim.x)
+    for (int t = threadIdx.x; t < (int)g.ndiff; t += blockDim.x)
       if (s_diff[t]) atomicAdd(&w.tile_diff[t], s_diff[t]);
 }
 
 __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_partial) {
-  const int ndiff = (g.ntx + 1) * (g.nty + 1);
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ndiff; t += gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.ndiff; t += stride)
     w.tile_diff[t] = 0;
-    if (t < g.ntiles) {
-      w.tile_wlo[t] = 0x7fffffff;
-      w.tile_whi[t] = -1;
-    }
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.ntiles; t += stride) {
+    w.tile_wlo[t] = 0x7fffffff;
+    w.tile_whi[t] = -1;
+  }
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < g.ngal; k += stride) {
+    GalState z;
+    z.dec = 0;
+    z.wmax = 0;
+    z.wbound_bits = z.sbound_bits = z.invw_bits = 0u;
+    z.pad_[0] = z.pad_[1] = z.pad_[2] = 0;
+    w.gst[k] = z;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     WsHeader* h = w.hdr;
     h->status = 0;
     h->item_counter = 0;
     h->reduce_counter = 0;
-    h->edges_dec = 0;
     h->n_pairs = h->n_items = h->n_partial_items = h->partial_bound = 0;
     h->cap_pairs = cap_pairs;
     h->cap_partial_items = cap_partial;
-    h->wmax = 0;
-    h->wbound_bits = 0u;
-    h->sbound_bits = 0u;
-    h->invw_bits = 0u;
     h->spec_bound = 0;
     h->n_spec = 0;
     h->spec_ready = 0;
+    h->kch = KCH_MIN;
   }
 }
 
-// Single-block pass over tiles after the histogram: per-tile counts from the
-// difference array (prefix sums along ty, then along tx; in shared memory
-// when it fits in `smem_cap` ints, else in place), pair offsets of the
-// tile-major list and an upper bound on split-K partial items (every segment
-// of a tile holds at most the tile's count).
-__global__ void k_plan_tiles(Geo g, Ws w, int smem_cap, int num_sms) {
-  constexpr int NT = 1024;
-  __shared__ long long s_a[NT], s_b[NT];
+// Channel edges of every cube as double-float pairs, inverse channel widths,
+// edge direction and the strict-monotonicity check of
+// spectral_models.py:180-187.  Batch-wide edge index e = edge0 + k.
+__global__ void k_edges(Geo g, Ws w) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < g.nedge;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int gk = find_gal(w.ge0, g.ngal, (int)e);
+    const Gal& G = w.gal[gk];
+    const int k = (int)e - G.edge0;
+    const double* ed = G.edges;
+    const int dec = ed[G.nc] < ed[0];
+    if (k == 0) w.gst[gk].dec = dec;
+    const double v = ed[k];
+    const float hi = (float)v;
+    w.ehi[e] = hi;
+    w.elo[e] = (float)(v - (double)hi);
+    if (k < G.nc) {
+      const float iw = (float)(1.0 / fabs(ed[k + 1] - ed[k]));
+      w.inv_w[e] = iw;
+      atomicMax(&w.gst[gk].invw_bits, __float_as_uint(iw));
+      const bool mono = dec ? (ed[k + 1] < ed[k]) : (ed[k + 1] > ed[k]);
+      if (!mono) atomicOr(&w.hdr->status, ST_EDGES);
+    } else {
+      w.inv_w[e] = 0.f;
+    }
+  }
+}
+
+// One block per cube: exact per-tile counts from the cube's difference array
+// (prefix sums along ty, then along tx; in shared memory when it fits in
+// `smem_cap` ints, else in place).
+__global__ void k_diff_prefix(Geo g, Ws w, int smem_cap) {
   extern __shared__ int s_d[];
-  const int tid = threadIdx.x;
-  {
-    const int dw = g.nty + 1, dh = g.ntx + 1;
-    const int ndiff = dw * dh;
-    const bool in_smem = ndiff <= smem_cap;
-    int* const d = in_smem ? s_d : w.tile_diff;
-    if (in_smem)
-      for (int e = tid; e < ndiff; e += NT) s_d[e] = w.tile_diff[e];
-    __syncthreads();
-    for (int r = tid; r < dh; r += NT) {
-      int acc = 0;
-      for (int c = 0; c < dw; ++c) {
-        acc += d[r * dw + c];
-        d[r * dw + c] = acc;
-      }
-    }
-    __syncthreads();
-    for (int c = tid; c < dw; c += NT) {
-      int acc = 0;
-      for (int r = 0; r < dh; ++r) {
-        acc += d[r * dw + c];
-        d[r * dw + c] = acc;
-      }
-    }
-    __syncthreads();
-    for (int t = tid; t < g.ntiles; t += NT) {
-      const int tx = t / g.nty, ty = t - tx * g.nty;
-      w.tile_count[t] = d[tx * dw + ty];
-    }
-    __syncthreads();
-  }
-  const int per = (g.ntiles + NT - 1) / NT;
-  const int t0 = tid * per;
-  const int t1 = min(g.ntiles, t0 + per);
-  long long sa = 0, sb = 0;
-  for (int t = t0; t < t1; ++t) sa += w.tile_count[t];
-  s_a[tid] = sa;
+  const Gal& G = w.gal[blockIdx.x];
+  const int dw = G.nty + 1, dh = G.ntx + 1;
+  const int nd = dw * dh;
+  const bool in_smem = nd <= smem_cap;
+  int* const d = in_smem ? s_d : w.tile_diff + G.diff0;
+  const int* src = w.tile_diff + G.diff0;
+  if (in_smem)
+    for (int e = threadIdx.x; e < nd; e += blockDim.x) s_d[e] = src[e];
   __syncthreads();
-  for (int off = 1; off < NT; off <<= 1) {
-    long long a = 0;
-    if (tid >= off) a = s_a[tid - off];
-    __syncthreads();
-    s_a[tid] += a;
-    __syncthreads();
+  for (int r = threadIdx.x; r < dh; r += blockDim.x) {
+    int acc = 0;
+    for (int c = 0; c < dw; ++c) {
+      acc += d[r * dw + c];
+      d[r * dw + c] = acc;
+    }
   }
-  // item size from the total, then the split-K bound with it
-  const int kch = item_particles(s_a[NT - 1], num_sms);
-  for (int t = t0; t < t1; ++t) {
-    const int cnt = w.tile_count[t];
-    const int nk = (cnt + kch - 1) / kch;
-    if (nk > 1) sb += (long long)nk * w.ncb_seg;
-  }
-  s_b[tid] = sb;
   __syncthreads();
-  for (int off = NT / 2; off > 0; off >>= 1) {
-    if (tid < off) s_b[tid] += s_b[tid + off];
-    __syncthreads();
+  for (int c = threadIdx.x; c < dw; c += blockDim.x) {
+    int acc = 0;
+    for (int r = 0; r < dh; ++r) {
+      acc += d[r * dw + c];
+      d[r * dw + c] = acc;
+    }
   }
-  long long ea = s_a[tid] - sa;
-  for (int t = t0; t < t1; ++t) {
-    w.tile_off[t] = ea;
-    ea += w.tile_count[t];
-  }
-  if (tid == NT - 1) {
-    w.tile_off[g.ntiles] = s_a[NT - 1];
-    WsHeader* h = w.hdr;
-    h->n_pairs = s_a[NT - 1];
-    h->partial_bound = s_b[0];
-    h->kch = kch;
-    unsigned st = h->status & ST_EDGES;
-    if (h->n_pairs > h->cap_pairs) st |= ST_PAIRS;
-    h->status = st;
+  __syncthreads();
+  for (int t = threadIdx.x; t < G.ntiles; t += blockDim.x) {
+    const int tx = t / G.nty, ty = t - tx * G.nty;
+    w.tile_count[G.tile0 + t] = d[tx * dw + ty];
   }
 }
 
-// Pairs in particle order: key = tile << cbits | clo, value = particle id.
-__global__ void k_emit(long long n, Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict__ vals) {
+// After the scan of the tile counts (total in tile_off[ntiles]): the work
+// item size from the total, the split-K bound with it (every segment of a
+// tile holds at most the tile's count) and the pair-capacity check.
+__global__ void k_plan_finish(Geo g, Ws w, int num_sms) {
+  __shared__ long long red[256];
+  const long long total = w.tile_off[g.ntiles];
+  const int kch = item_particles(total, num_sms);
+  long long sb = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.ntiles; t += gridDim.x * blockDim.x) {
+    const long long cnt = w.tile_off[t + 1] - w.tile_off[t];
+    const long long nk = (cnt + kch - 1) / kch;
+    if (nk > 1) sb += nk * w.gal[find_gal(w.gt0, g.ngal, t)].ncb;
+  }
+  red[threadIdx.x] = sb;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && red[0])
+    atomicAdd(reinterpret_cast<unsigned long long*>(&w.hdr->partial_bound),
+              (unsigned long long)red[0]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    WsHeader* h = w.hdr;
+    h->n_pairs = total;
+    h->kch = kch;
+    if (total > h->cap_pairs) atomicOr(&h->status, ST_PAIRS);
+  }
+}
+
+// Pairs in particle order: key = global tile << cbits | clo, value = particle.
+__global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict__ vals) {
   if (w.hdr->status & (ST_PAIRS | ST_EDGES)) return;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-       p += (long long)gridDim.x * blockDim.x) {
-    const PRec rec = w.rec[p];
+  for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < g.n;
+       P += (long long)gridDim.x * blockDim.x) {
+    const PRec rec = w.rec[P];
     if (rec.ilo > rec.ihi) continue;
-    long long o = w.pair_off[p];
+    const Gal& G = w.gal[find_gal(w.gp0, g.ngal, P)];
+    long long o = w.pair_off[P];
     const int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
     const int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
     for (int tx = tx0; tx <= tx1; ++tx)
       for (int ty = ty0; ty <= ty1; ++ty) {
-        const unsigned t = (unsigned)(tx * g.nty + ty);
-        keys[o] = (t << w.cbits) | (unsigned)rec.clo;
-        vals[o] = (int)p;
+        const unsigned t = (unsigned)(G.tile0 + tx * G.nty + ty);
+        keys[o] = (t << g.cbits) | (unsigned)rec.clo;
+        vals[o] = (int)P;
         ++o;
       }
   }
@@ -394,24 +452,27 @@ __device__ __forceinline__ long long lower_bound_keys(const unsigned* keys, long
 // [c0 - wmax, c0 + width)), its K chunks and its split-K partial items.
 __global__ void k_segments(Geo g, Ws w) {
   const bool bad = (w.hdr->status & (ST_PAIRS | ST_EDGES)) != 0;
-  const int wmax = w.hdr->wmax;
   const int kch = w.hdr->kch;
-  const unsigned cmask_hi = (1u << w.cbits);
-  for (int sg = blockIdx.x * blockDim.x + threadIdx.x; sg < w.nseg; sg += gridDim.x * blockDim.x) {
-    const int t = sg / w.ncb_seg;
-    const int cb = sg - t * w.ncb_seg;
+  const unsigned cmask_hi = (1u << g.cbits);
+  for (int sg = blockIdx.x * blockDim.x + threadIdx.x; sg < g.nseg; sg += gridDim.x * blockDim.x) {
+    const int gk = find_gal(w.gs0, g.ngal, sg);
+    const Gal& G = w.gal[gk];
+    const int ls = sg - G.seg0;
+    const int t = G.tile0 + ls / G.ncb;
+    const int cb = ls - (ls / G.ncb) * G.ncb;
     long long lo = w.tile_off[t], hi = w.tile_off[t + 1];
     int items = 0, part = 0;
     if (!bad && hi > lo) {
-      if (w.ncb_seg > 1) {
-        const int c0 = cb * w.seg_width;
+      if (G.ncb > 1) {
+        const int wmax = w.gst[gk].wmax;
+        const int c0 = cb * G.width;
         const int clo_min = c0 - wmax > 0 ? c0 - wmax : 0;
-        const unsigned c_end = (unsigned)(c0 + w.seg_width);  // first clo past the block
-        const unsigned tk = (unsigned)t << w.cbits;
+        const unsigned c_end = (unsigned)(c0 + G.width);  // first clo past the block
+        const unsigned tk = (unsigned)t << g.cbits;
         const long long a = lower_bound_keys(w.keys, lo, hi, tk | (unsigned)clo_min);
         const long long b = c_end >= cmask_hi ? hi : lower_bound_keys(w.keys, a, hi, tk | c_end);
         // skip blocks entirely outside the tile's channel window
-        if (c0 > w.tile_whi[t] || c0 + w.seg_width <= w.tile_wlo[t]) {
+        if (c0 > w.tile_whi[t] || c0 + G.width <= w.tile_wlo[t]) {
           lo = hi = a;
         } else {
           lo = a;
@@ -436,83 +497,67 @@ __global__ void k_check_partials(Ws w) {
   if (h->n_partial_items > h->cap_partial_items) h->status |= ST_PARTIALS;
 }
 
-// Channel edges as double-float pairs, inverse channel widths, edge
-// direction and the strict-monotonicity check of spectral_models.py:180-187.
-__global__ void k_edges(const double* e, int nc, Ws w) {
-  const int dec = e[nc] < e[0];
-  if (blockIdx.x == 0 && threadIdx.x == 0) w.hdr->edges_dec = dec;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= nc; k += gridDim.x * blockDim.x) {
-    double v = e[k];
-    float hi = (float)v;
-    w.ehi[k] = hi;
-    w.elo[k] = (float)(v - (double)hi);
-    if (k < nc) {
-      w.inv_w[k] = (float)(1.0 / fabs(e[k + 1] - e[k]));
-      atomicMax(&w.hdr->invw_bits, __float_as_uint(w.inv_w[k]));
-      bool mono = dec ? (e[k + 1] < e[k]) : (e[k + 1] > e[k]);
-      if (!mono) atomicOr(&w.hdr->status, ST_EDGES);
-    }
-  }
-}
-
 static unsigned grid_for(long long n, int num_sms) {
   long long blocks = (n + 255) / 256;
   if (blocks > (long long)num_sms * 32) blocks = (long long)num_sms * 32;
   return (unsigned)(blocks > 0 ? blocks : 1);
 }
 
-// Records, tile histogram, per-particle pair offsets and the tile plan.
-void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cudaStream_t s,
-                 long long cap_pairs, long long cap_partial) {
-  k_tile_init<<<(g.ntiles + 255) / 256, 256, 0, s>>>(g, w, cap_pairs, cap_partial);
-  k_edges<<<(g.nc + 256) / 256, 256, 0, s>>>(a.edges, g.nc, w);
-  if (a.n > 0) {
-    // with the histogram in shared memory every block flushes up to ntiles
-    // counts: fewer, longer-lived blocks
-    const size_t ndiff = (size_t)(g.ntx + 1) * (g.nty + 1);
-    const bool smem_hist = ndiff <= (size_t)PREP_SMEM_DIFF;
-    const size_t hist_bytes = smem_hist ? sizeof(int) * ndiff : 0;
-    unsigned blocks = grid_for(a.n, num_sms);
+// Records, tile histograms, per-particle pair offsets and the tile plan.
+void launch_prep(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, long long cap_pairs,
+                 long long cap_partial) {
+  long long init_n = g.ndiff > g.ntiles ? g.ndiff : g.ntiles;
+  if (g.ngal > init_n) init_n = g.ngal;
+  k_tile_init<<<grid_for(init_n, num_sms), 256, 0, s>>>(g, w, cap_pairs, cap_partial);
+  k_edges<<<grid_for(g.nedge, num_sms), 256, 0, s>>>(g, w);
+  if (g.n > 0) {
+    // with the histogram in shared memory every block flushes the array:
+    // fewer, longer-lived blocks
+    const bool smem_hist = g.ngal == 1 && g.ndiff <= PREP_SMEM_DIFF;
+    const size_t hist_bytes = smem_hist ? sizeof(int) * (size_t)g.ndiff : 0;
+    unsigned blocks = grid_for(g.n, num_sms);
     const unsigned per_sm = hist_bytes <= 16384 ? 8u : 4u;
     if (smem_hist && blocks > per_sm * (unsigned)num_sms) blocks = per_sm * (unsigned)num_sms;
-    k_prep<<<blocks, PREP_THREADS, hist_bytes, s>>>(a, g, w);
+    k_prep<<<blocks, PREP_THREADS, hist_bytes, s>>>(g, w);
   }
-  launch_scan(w.npairs, a.n, w.pair_off, w.scan_sums, nullptr, s);
-  // dynamic shared memory for the difference array: up to 200 KB
-  // (the attribute is per device: set on every launch, a host-side call)
+  launch_scan(w.npairs, g.n, w.pair_off, w.scan_sums, nullptr, s);
+  // per-cube prefix sums of the difference arrays, in up to 200 KB of
+  // dynamic shared memory (the attribute is per device: set on every launch)
   constexpr int kPlanSmemCap = 50 * 1024;
-  const long long ndiff_all = (long long)(g.ntx + 1) * (g.nty + 1);
-  int cap = ndiff_all <= kPlanSmemCap ? (int)ndiff_all : 0;
-  if (cap > 0 && cudaFuncSetAttribute(k_plan_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(int) * kPlanSmemCap)) != cudaSuccess) {
+  int cap = g.max_diff <= kPlanSmemCap ? g.max_diff : 0;
+  if (cap > 12 * 1024 &&
+      cudaFuncSetAttribute(k_diff_prefix, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(int) * kPlanSmemCap)) != cudaSuccess) {
     cudaGetLastError();  // fall back to the in-place prefix sums
     cap = 0;
   }
-  k_plan_tiles<<<1, 1024, sizeof(int) * (size_t)cap, s>>>(g, w, cap, num_sms);
+  k_diff_prefix<<<g.ngal, 256, sizeof(int) * (size_t)cap, s>>>(g, w, cap);
+  launch_scan(w.tile_count, g.ntiles, w.tile_off, w.scan_sums, w.tile_off + g.ntiles, s);
+  k_plan_finish<<<grid_for(g.ntiles, num_sms), 256, 0, s>>>(g, w, num_sms);
 }
 
-int sort_bits(const Geo& g, const Ws& w) {
+int sort_bits(const Geo& g) {
   int tbits = 0;
   while ((1LL << tbits) < (long long)g.ntiles) ++tbits;
-  return tbits + w.cbits;
+  return tbits + g.cbits;
 }
 
 // Tile-major list sorted by (tile, clo), then the segments with their
 // work-item and partial offsets.  Pairs are emitted into the buffer from
 // which an even/odd number of radix passes ends in w.keys / w.list.
-void launch_sort_segments(const PrepArgs& a, const Geo& g, const Ws& w, long long cap_pairs,
-                          int num_sms, cudaStream_t s) {
-  const int passes = (sort_bits(g, w) + 7) / 8;
+void launch_sort_segments(const Geo& g, const Ws& w, long long cap_pairs, int num_sms,
+                          cudaStream_t s) {
+  const int passes = (sort_bits(g) + 7) / 8;
   unsigned* k0 = (passes & 1) ? w.keys_tmp : w.keys;
   int* v0 = (passes & 1) ? w.list_tmp : w.list;
   unsigned* k1 = (passes & 1) ? w.keys : w.keys_tmp;
   int* v1 = (passes & 1) ? w.list : w.list_tmp;
-  if (a.n > 0) k_emit<<<grid_for(a.n, num_sms), 256, 0, s>>>(a.n, g, w, k0, v0);
-  launch_radix_sort(k0, v0, k1, v1, &w.hdr->n_pairs, cap_pairs, sort_bits(g, w), w.rs_hist,
+  if (g.n > 0) k_emit<<<grid_for(g.n, num_sms), 256, 0, s>>>(g, w, k0, v0);
+  launch_radix_sort(k0, v0, k1, v1, &w.hdr->n_pairs, cap_pairs, sort_bits(g), w.rs_hist,
                     w.rs_off, w.scan_sums, num_sms, s);
-  k_segments<<<(unsigned)((w.nseg + 255) / 256), 256, 0, s>>>(g, w);
-  launch_scan(w.seg_items, w.nseg, w.item_off, w.scan_sums, &w.hdr->n_items, s);
-  launch_scan(w.seg_part, w.nseg, w.part_off, w.scan_sums, &w.hdr->n_partial_items, s);
+  k_segments<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, w);
+  launch_scan(w.seg_items, g.nseg, w.item_off, w.scan_sums, &w.hdr->n_items, s);
+  launch_scan(w.seg_part, g.nseg, w.part_off, w.scan_sums, &w.hdr->n_partial_items, s);
   k_check_partials<<<1, 1, 0, s>>>(w);
 }
 

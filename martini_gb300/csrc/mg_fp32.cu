@@ -24,7 +24,7 @@ __device__ __forceinline__ int find_segment(const long long* item_off, int nseg,
 }
 
 struct ItemInfo {
-  int seg, tile, tx, ty, kc, nk;
+  int seg, gal, tile, tx, ty, kc, nk;  // tile: within the cube
   int c0;            // first channel of this item's block
   long long lbeg;    // particle list range
   int lcount;
@@ -33,15 +33,18 @@ struct ItemInfo {
 __device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long long item,
                                                 int kch) {
   ItemInfo it;
-  const int sg = find_segment(w.item_off, w.nseg, item);
+  const int sg = find_segment(w.item_off, g.nseg, item);
   it.seg = sg;
-  it.tile = sg / w.ncb_seg;
-  const int cb = sg - it.tile * w.ncb_seg;
-  it.tx = it.tile / g.nty;
-  it.ty = it.tile - it.tx * g.nty;
+  it.gal = find_gal(w.gs0, g.ngal, sg);
+  const Gal& G = w.gal[it.gal];
+  const int ls = sg - G.seg0;
+  it.tile = ls / G.ncb;
+  const int cb = ls - it.tile * G.ncb;
+  it.tx = it.tile / G.nty;
+  it.ty = it.tile - it.tx * G.nty;
   it.nk = w.seg_items[sg];
   it.kc = (int)(item - w.item_off[sg]);
-  it.c0 = cb * w.seg_width;
+  it.c0 = cb * G.width;
   it.lbeg = w.seg_lo[sg] + (long long)it.kc * kch;
   const long long left = w.seg_hi[sg] - it.lbeg;
   it.lcount = (int)(left < kch ? left : kch);
@@ -49,7 +52,7 @@ __device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long 
 }
 
 __global__ void __launch_bounds__(F32_THREADS, 2)
-k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict__ cube) {
+k_contract_fp32(Geo g, Ws w) {
   __shared__ __align__(16) float Ws_[F32_KC][TILE_PX];
   __shared__ __align__(16) float Ss_[F32_KC][CBLK];
   __shared__ PRec recs[F32_KC];
@@ -62,7 +65,6 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
   if (hdr->status) return;
   const long long n_items = hdr->n_items;
   const int kch = hdr->kch;
-  const int dec = hdr->edges_dec;
   const int tr = tid >> 4;  // pixel group: pixels tr*8 .. tr*8+7
   const int tc = tid & 15;  // channel group: channels tc*4 .. tc*4+3
 
@@ -73,6 +75,12 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
     __syncthreads();
     if (item >= n_items) break;
     const ItemInfo it = decode_item(g, w, item, kch);
+    const Gal& G = w.gal[it.gal];
+    const int dec = w.gst[it.gal].dec;
+    const int nc = G.nc;
+    const float* ehi = w.ehi + G.edge0;
+    const float* elo = w.elo + G.edge0;
+    const float* inv_w = w.inv_w + G.edge0;
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
 
     float acc[8][4];
@@ -108,11 +116,11 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
         for (int cc = ii * 8; cc < ii * 8 + 8; ++cc) {
           const int c = it.c0 + cc;
           float s = 0.f;
-          if (c < g.nc && q < kn) {
+          if (c < nc && q < kn) {
             if (g.spectral_model == MG_SPECTRUM_TABLE) {
-              s = spectra[(long long)r.pad_ * g.nc + c];
+              s = G.spectra[((long long)r.pad_ - G.p0) * nc + c];
             } else {
-              s = channel_spectrum(r, g.spectral_model, c, dec, w.ehi, w.elo, w.inv_w);
+              s = channel_spectrum(r, g.spectral_model, c, dec, ehi, elo, inv_w);
             }
           }
           Ss_[q][cc] = s;
@@ -142,17 +150,17 @@ k_contract_fp32(Geo g, Ws w, const float* __restrict__ spectra, float* __restric
       for (int a = 0; a < 8; ++a) {
         const int px = tr * 8 + a;
         const int i = i0 + px / TILE_J, j = j0 + px % TILE_J;
-        if (i >= g.nx || j >= g.ny) continue;
-        float* dst = cube + ((long long)i * g.ny + j) * g.nc;
+        if (i >= G.nx || j >= G.ny) continue;
+        float* dst = G.cube + ((long long)i * G.ny + j) * nc;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
           const int c = it.c0 + tc * 4 + b;
-          if (c < g.nc) dst[c] = g.accumulate ? dst[c] + acc[a][b] : acc[a][b];
+          if (c < nc) dst[c] = g.accumulate ? dst[c] + acc[a][b] : acc[a][b];
         }
       }
     } else {
       const long long slot = w.part_off[it.seg] + it.kc;
-      float* dst = w.partial + slot * (TILE_PX * CBLK);
+      float* dst = w.partial + slot * (long long)(TILE_PX * g.max_width);
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
         const int px = tr * 8 + a;
@@ -172,22 +180,24 @@ constexpr int RED_THREADS = 256;
 constexpr int RED_CHUNK = RED_THREADS * 4;
 constexpr int RED_ROWS = 8;
 
-__global__ void __launch_bounds__(RED_THREADS) k_reduce_partials(Geo g, Ws w,
-                                                                 float* __restrict__ cube) {
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_partials(Geo g, Ws w) {
   if (w.hdr->status) return;
-  const int width = w.seg_width;       // a multiple of 16 channels
-  const int per_row = TILE_PX * width;
-  const int nchunk = (per_row + RED_CHUNK - 1) / RED_CHUNK;
-  const long long units = (long long)w.nseg * nchunk;
+  const long long slot = (long long)TILE_PX * g.max_width;  // floats per partial row
+  const int nchunk = (int)((slot + RED_CHUNK - 1) / RED_CHUNK);
+  const long long units = (long long)g.nseg * nchunk;
   for (long long u = blockIdx.x; u < units; u += gridDim.x) {
     const int sg = (int)(u / nchunk);
     const int nk = w.seg_part[sg];
     if (nk == 0) continue;
+    const int gk = find_gal(w.gs0, g.ngal, sg);
+    const Gal& G = w.gal[gk];
+    const int width = G.width;  // a multiple of 16 channels
+    const int per_row = TILE_PX * width;
     const int e = (int)(u - (long long)sg * nchunk) * RED_CHUNK + threadIdx.x * 4;
     if (e >= per_row) continue;
     const float4* src =
-        reinterpret_cast<const float4*>(w.partial + w.part_off[sg] * (long long)per_row + e);
-    const long long row4 = per_row / 4;
+        reinterpret_cast<const float4*>(w.partial + w.part_off[sg] * slot + e);
+    const long long row4 = slot / 4;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k0 = 0; k0 < nk; k0 += RED_ROWS) {
       float4 v[RED_ROWS];
@@ -203,28 +213,30 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partials(Geo g, Ws w,
           acc.w += v[q].w;
         }
     }
-    const int t = sg / w.ncb_seg;
-    const int cb = sg - t * w.ncb_seg;
-    const int tx = t / g.nty, ty = t - tx * g.nty;
+    const int ls = sg - G.seg0;
+    const int t = ls / G.ncb;
+    const int cb = ls - t * G.ncb;
+    const int tx = t / G.nty, ty = t - tx * G.nty;
     const int px = e / width, c = cb * width + (e - px * width);
     const int i = tx * TILE_I + px / TILE_J, j = ty * TILE_J + px % TILE_J;
-    if (i >= g.nx || j >= g.ny) continue;
-    float* dst = cube + ((long long)i * g.ny + j) * g.nc + c;
+    if (i >= G.nx || j >= G.ny) continue;
+    const int nc = G.nc;
+    float* dst = G.cube + ((long long)i * G.ny + j) * nc + c;
     if (g.accumulate) {
-      if (c < g.nc) acc.x += dst[0];
-      if (c + 1 < g.nc) acc.y += dst[1];
-      if (c + 2 < g.nc) acc.z += dst[2];
-      if (c + 3 < g.nc) acc.w += dst[3];
+      if (c < nc) acc.x += dst[0];
+      if (c + 1 < nc) acc.y += dst[1];
+      if (c + 2 < nc) acc.z += dst[2];
+      if (c + 3 < nc) acc.w += dst[3];
     }
-    if (c < g.nc) dst[0] = acc.x;
-    if (c + 1 < g.nc) dst[1] = acc.y;
-    if (c + 2 < g.nc) dst[2] = acc.z;
-    if (c + 3 < g.nc) dst[3] = acc.w;
+    if (c < nc) dst[0] = acc.x;
+    if (c + 1 < nc) dst[1] = acc.y;
+    if (c + 2 < nc) dst[2] = acc.z;
+    if (c + 3 < nc) dst[3] = acc.w;
   }
 }
 
-void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms, cudaStream_t s) {
-  k_reduce_partials<<<num_sms * 8, RED_THREADS, 0, s>>>(g, w, cube);
+void launch_reduce_partials(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
+  k_reduce_partials<<<num_sms * 8, RED_THREADS, 0, s>>>(g, w);
 }
 
 // FP64 flux sums over the unpadded region (martini/martini.py:367-392):
@@ -281,10 +293,55 @@ void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, 
   k_flux_final<<<1, 1024, 0, s>>>(part, nch, nc, flux);
 }
 
-void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
-                          int num_sms, cudaStream_t s) {
-  k_contract_fp32<<<num_sms * 2, F32_THREADS, 0, s>>>(g, w, spectra, cube);
-  launch_reduce_partials(g, w, cube, num_sms, s);
+void launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
+  k_contract_fp32<<<num_sms * 2, F32_THREADS, 0, s>>>(g, w);
+  launch_reduce_partials(g, w, num_sms, s);
+}
+
+// FP64 flux sums of every cube of a batch: one block per unpadded pixel row
+// of all cubes (a thread per channel, voxels widened to FP64 and added in
+// row order), then one block per cube summing its rows in row order.
+__global__ void k_flux_rows(Geo g, Ws w) {
+  const int gk = find_gal(w.gr0, g.ngal, (int)blockIdx.x);
+  const Gal& G = w.gal[gk];
+  if (!G.flux) return;
+  const int r = blockIdx.x - G.row0;
+  const int i = G.padx + r;
+  const int nc = G.nc;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const float* row = G.cube + ((long long)i * G.ny) * nc + c;
+    double acc = 0.0;
+    for (int j = G.pady; j < G.ny - G.pady; ++j) acc += (double)__ldcs(row + (long long)j * nc);
+    w.flux_part[G.fpart0 + (long long)r * nc + c] = acc;
+  }
+}
+
+__global__ void k_flux_cubes(Geo g, Ws w) {
+  __shared__ double red[256];
+  const Gal& G = w.gal[blockIdx.x];
+  if (!G.flux) return;
+  const int rows = G.nx - 2 * G.padx;
+  double tot = 0.0;
+  for (int c = threadIdx.x; c < G.nc; c += blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < rows; ++r) s += w.flux_part[G.fpart0 + (long long)r * G.nc + c];
+    G.flux[1 + c] = s;
+    tot += s;
+  }
+  red[threadIdx.x] = tot;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) G.flux[0] = red[0];
+}
+
+void launch_flux_batch(const Geo& g, const Ws& w, cudaStream_t s) {
+  if (g.nrows <= 0) return;
+  const int thr = g.max_nc < 256 ? ((g.max_nc + 31) / 32) * 32 : 256;
+  k_flux_rows<<<g.nrows, thr, 0, s>>>(g, w);
+  k_flux_cubes<<<g.ngal, 256, 0, s>>>(g, w);
 }
 
 }  // namespace mg

@@ -56,18 +56,82 @@ struct KSpec {
   float pad_;
 };
 
-// Device-side problem constants (copied into kernel parameters).
-struct Geo {
-  int nx, ny, nc;
-  int padx, pady;
+// One cube of a batch (mg_insert is a batch of one).  Written into the
+// workspace by k_set_gals from kernel parameters, so an insertion needs no
+// host-to-device copy and can be captured in a CUDA graph.  Offsets place the
+// cube's particles, tiles, segments, edges and flux rows in the batch-wide
+// arrays.
+struct Gal {
+  const double* x;
+  const double* y;
+  const double* r;
+  const float* h;
+  const int8_t* kidx;
+  const double* v;
+  const float* sigma;
+  const double* amp;
+  const float* spectra;
+  const double* edges;
+  float* cube;
+  double* flux;
+  long long p0;       // first particle in the batch
+  long long n;        // particles
+  long long diff0;    // first entry of the tile difference array
+  long long fpart0;   // first FP64 flux partial (flux rows x nc)
+  int nx, ny, nc, padx, pady;
   int ntx, nty, ntiles;
+  int tile0;          // first global tile
+  int seg0;           // first global segment
+  int ncb, width;     // channel blocks per tile and channels per block
+  int edge0;          // first channel edge (nc + 1 per cube)
+  int row0;           // first flux row (unpadded rows of the cubes before)
+  float sigma_const;
+  int pad_;
+};
+
+// Per-cube values the kernels find on the device (reset by k_tile_init).
+struct GalState {
+  int dec;                 // channel edges decrease with index
+  int wmax;                // max (chi - clo) over the cube's particles
+  unsigned wbound_bits;    // max pixel weight bound (float bits, >= 0)
+  unsigned sbound_bits;    // max spectrum bound (float bits, >= 0)
+  unsigned invw_bits;      // max 1 / |channel width| (float bits)
+  int pad_[3];
+};
+
+// Batch-wide constants (kernel parameters).  Every cube of a batch shares
+// the kernel table, spectral model, contraction form and accumulate flag.
+struct Geo {
+  int ngal;
   int n_kernels;
   int spectral_model;
-  float sigma_const;
   int form;
-  int accumulate;    // add into the cube instead of overwriting it
+  int accumulate;     // add into the cubes instead of overwriting them
+  int ntiles;         // tiles of all cubes
+  int nseg;           // segments of all cubes
+  int max_width;      // widest channel block (partial slots hold TILE_PX x max_width)
+  int max_nc;
+  int cbits;          // channel bits of the sort key (widest band)
+  int nrows;          // flux rows of all cubes
+  int max_diff;       // largest difference array of one cube
+  long long n;        // particles of all cubes
+  long long ndiff;    // difference-array entries of all cubes
+  long long nedge;    // channel edges of all cubes
+  long long nfpart;   // FP64 flux partials of all cubes
   KSpec ks[MG_MAX_KERNELS];
 };
+
+// Cube of a batch-wide index: the largest k < ngal with keys[k] <= v (cubes
+// with no particles share their successor's start, and are skipped).
+template <typename T>
+__device__ __forceinline__ int find_gal(const T* keys, int ngal, T v) {
+  int a = 0, b = ngal;
+  while (b - a > 1) {
+    const int m = (a + b) >> 1;
+    if (keys[m] <= v) a = m; else b = m;
+  }
+  return a;
+}
 
 // Status bits of WsHeader::status.
 constexpr unsigned ST_PAIRS = 1u;        // pairs exceed the list capacity
@@ -80,17 +144,13 @@ struct WsHeader {
   unsigned int status;           // ST_* bits
   unsigned int item_counter;     // dynamic scheduler cursor
   unsigned int reduce_counter;
-  int edges_dec;                 // 1 if channel edges decrease with index
+  int pad0;
   long long n_pairs;
   long long n_items;
   long long n_partial_items;
   long long partial_bound;       // upper bound on partial items (from tile counts)
   long long cap_pairs;
   long long cap_partial_items;
-  int wmax;                      // max (chi - clo) over particles
-  unsigned wbound_bits;          // max pixel weight bound (float bits, >= 0)
-  unsigned sbound_bits;          // max spectrum bound (float bits, >= 0)
-  unsigned invw_bits;            // max 1 / |channel width| (float bits)
   long long spec_bound;          // sum over particles of support channels (Gaussian)
   long long n_spec;              // values in the spectrum store (spectrum stage)
   int spec_ready;                // 1 once the store holds this binning's spectra
@@ -98,22 +158,31 @@ struct WsHeader {
   long long pad1[1];
 };
 
-// Pointers into the workspace (host computes, passes by value).  A
-// "segment" is one (tile, channel block) of the contraction: ncb_seg blocks
-// per tile (FP32 form: ceil(nc / CBLK); tensor-core form: 1, the full band).
+// Pointers into the workspace (host computes, passes by value).  Arrays run
+// over the whole batch.  A "segment" is one (tile, channel block) of the
+// contraction: Gal::ncb blocks per tile (FP32 form: ceil(nc / CBLK) blocks
+// of CBLK channels; tensor-core forms: the band rounded to 16 in one block up
+// to 256 channels, else blocks of 256).
 struct Ws {
   WsHeader* hdr;
+  Gal* gal;              // [ngal]
+  GalState* gst;         // [ngal]
+  long long* gp0;        // [ngal + 1] first particle of each cube
+  int* gt0;              // [ngal + 1] first tile
+  int* gs0;              // [ngal + 1] first segment
+  int* ge0;              // [ngal + 1] first edge
+  int* gr0;              // [ngal + 1] first flux row
   PRec* rec;             // [n]
   int* npairs;           // [n] tiles touched per particle
   long long* pair_off;   // [n] exclusive scan of npairs
   int* tile_count;       // [ntiles]
-  int* tile_diff;        // [(ntx + 1) * (nty + 1)] 2D difference array of tile coverage
+  int* tile_diff;        // [ndiff] per cube (ntx + 1) x (nty + 1) difference arrays
   int* tile_wlo;         // [ntiles]
   int* tile_whi;         // [ntiles]
   long long* tile_off;   // [ntiles + 1] pair offsets (tile-major sorted list)
-  float* ehi;            // [nc + 1] edges, double-float high part
-  float* elo;            // [nc + 1] low part
-  float* inv_w;          // [nc] 1 / |channel width|
+  float* ehi;            // [nedge] edges, double-float high part
+  float* elo;            // [nedge] low part
+  float* inv_w;          // [nedge] 1 / |channel width| (channel c of a cube at edge0 + c)
   unsigned* keys;        // [cap_pairs] sorted keys: tile << cbits | clo
   int* list;             // [cap_pairs] particle ids in sorted order
   unsigned* keys_tmp;    // [cap_pairs] radix-sort second buffer
@@ -127,37 +196,19 @@ struct Ws {
   int* seg_part;         // [nseg] partial items of each segment
   long long* item_off;   // [nseg] exclusive scan of seg_items
   long long* part_off;   // [nseg] exclusive scan of seg_part
-  float* partial;        // [cap_partial_items][TILE_PX][seg_width]
-  double* flux_part;     // [flux_chunks][nc]
+  float* partial;        // [cap_partial_items][TILE_PX][max_width]
+  double* flux_part;     // [nfpart]
   float* spec;           // [cap_spec] per-particle Gaussian spectra over [clo, chi]
   long long cap_spec;    // room in spec (the workspace beyond the fixed layout)
-  int nseg;              // ntiles * ncb_seg
-  int ncb_seg;           // channel blocks per tile
-  int seg_width;         // channels per segment (CBLK or nc rounded up to 16)
-  int cbits;             // channel bits of the sort key
 };
 
-// Particle inputs of the prep kernel (device pointers from mg_problem).
-struct PrepArgs {
-  long long n;
-  const double* x;
-  const double* y;
-  const double* r;
-  const float* h;
-  const int8_t* kidx;
-  const double* v;
-  const float* sigma;
-  const double* amp;
-  const double* edges;
-  const float* spectra;
-};
-
-// Host-side launchers.
-void launch_prep(const PrepArgs& a, const Geo& g, const Ws& w, int num_sms, cudaStream_t s,
-                 long long cap_pairs, long long cap_partial);
-void launch_sort_segments(const PrepArgs& a, const Geo& g, const Ws& w, long long cap_pairs,
-                          int num_sms, cudaStream_t s);
-int sort_bits(const Geo& g, const Ws& w);
+// Host-side launchers (all asynchronous on stream s).
+void launch_set_gals(const Gal* gals, const Geo& g, const Ws& w, cudaStream_t s);
+void launch_prep(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, long long cap_pairs,
+                 long long cap_partial);
+void launch_sort_segments(const Geo& g, const Ws& w, long long cap_pairs, int num_sms,
+                          cudaStream_t s);
+int sort_bits(const Geo& g);
 void launch_scan(const int* in, long long n, long long* out, long long* sums, long long* total,
                  cudaStream_t s);
 long long scan_blocks(long long n);
@@ -165,12 +216,11 @@ long long radix_blocks(long long n);
 bool launch_radix_sort(unsigned* keys, int* vals, unsigned* kt, int* vt, const long long* np,
                        long long cap, int bits, int* hist, long long* off, long long* sums,
                        int num_sms, cudaStream_t s);
-void launch_contract_fp32(const Geo& g, const Ws& w, const float* spectra, float* cube,
-                          int num_sms, cudaStream_t s);
-int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
-                           int num_sms, cudaStream_t s);
-void launch_reduce_partials(const Geo& g, const Ws& w, float* cube, int num_sms, cudaStream_t s);
-void launch_spec_store(const Geo& g, const Ws& w, long long n, int num_sms, cudaStream_t s);
+void launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
+int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
+void launch_reduce_partials(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
+void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
+void launch_flux_batch(const Geo& g, const Ws& w, cudaStream_t s);
 void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, double* part,
                  double* flux, cudaStream_t s);
 int flux_chunks(int nx, int padx);

@@ -213,24 +213,27 @@ __device__ __forceinline__ float tc_spectrum(const PRec& r, int model, int c, in
 }
 
 struct ItemTC {
-  int seg, tile, tx, ty, kc, nk;
+  int seg, gal, tile, tx, ty, kc, nk;  // tile: within the cube
   int c0;  // first channel of the segment's block
   long long lbeg;
   int lcount;
 };
 
 __device__ __forceinline__ ItemTC decode_tc(const Geo& g, const Ws& w, long long item, int kch) {
-  int a = 0, b = w.nseg;
+  int a = 0, b = g.nseg;
   while (b - a > 1) {
     int m = (a + b) >> 1;
     if (w.item_off[m] <= item) a = m; else b = m;
   }
   ItemTC it;
   it.seg = a;
-  it.tile = a / w.ncb_seg;
-  it.c0 = (a - it.tile * w.ncb_seg) * w.seg_width;
-  it.tx = it.tile / g.nty;
-  it.ty = it.tile - it.tx * g.nty;
+  it.gal = find_gal(w.gs0, g.ngal, a);
+  const Gal& G = w.gal[it.gal];
+  const int ls = a - G.seg0;
+  it.tile = ls / G.ncb;
+  it.c0 = (ls - it.tile * G.ncb) * G.width;
+  it.tx = it.tile / G.nty;
+  it.ty = it.tile - it.tx * G.nty;
   it.nk = w.seg_items[a];
   it.kc = (int)(item - w.item_off[a]);
   it.lbeg = w.seg_lo[a] + (long long)it.kc * kch;
@@ -493,8 +496,8 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
 // Row lengths of the spectrum store: support channels of each particle
 // that reaches the cube (0 otherwise).  Written over the per-particle pair
 // counts, which the binning stage no longer needs.
-__global__ void k_spec_count(long long n, Ws w) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+__global__ void k_spec_count(Geo g, Ws w) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.n;
        p += (long long)gridDim.x * blockDim.x) {
     const PRec& r = w.rec[p];
     const int ilo = r.ilo, ihi = r.ihi, clo = r.clo, chi = r.chi;
@@ -507,18 +510,24 @@ __global__ void k_spec_count(long long n, Ws w) {
 // one warp per particle, the same shared-edge arithmetic as the producer, so
 // the contraction gives the same bits with or without the store.  Row p
 // starts at pair_off[p] (exclusive scan of the row lengths).
-__global__ void k_spec_eval(long long n, int nc, Ws w) {
+__global__ void k_spec_eval(Geo g, Ws w) {
   const bool fits = w.hdr->n_spec <= w.cap_spec;
   // read by the contraction, which runs after this whole kernel
   if (blockIdx.x == 0 && threadIdx.x == 0) w.hdr->spec_ready = fits ? 1 : 0;
   if (!fits) return;
-  const int dec = w.hdr->edges_dec;
   const int lane = threadIdx.x & 31;
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; p < n;
+  for (long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; p < g.n;
        p += nwarps) {
     const int cnt = w.npairs[p];
     if (cnt == 0) continue;  // warp-uniform
+    const int gk = find_gal(w.gp0, g.ngal, p);
+    const Gal& G = w.gal[gk];
+    const int dec = w.gst[gk].dec;
+    const int nc = G.nc;
+    const float* ehi = w.ehi + G.edge0;
+    const float* elo = w.elo + G.edge0;
+    const float* inv_w = w.inv_w + G.edge0;
     const PRec r = w.rec[p];
     float* out = w.spec + w.pair_off[p];
     for (int base = 0; base < cnt; base += 31) {
@@ -526,12 +535,12 @@ __global__ void k_spec_eval(long long n, int nc, Ws w) {
       const int c = r.clo + m;
       float ca = 0.f;
       bool pa = true;
-      if (m <= cnt && c <= nc) edge_term(r, c, w.ehi, w.elo, ca, pa);
+      if (m <= cnt && c <= nc) edge_term(r, c, ehi, elo, ca, pa);
       const float cb = __shfl_down_sync(0xffffffffu, ca, 1);
       const bool pb = __shfl_down_sync(0xffffffffu, (int)pa, 1) != 0;
       if (lane < 31 && m < cnt) {
         const float phi = dec ? half_diff_from_c(cb, pb, ca, pa) : half_diff_from_c(ca, pa, cb, pb);
-        out[m] = r.amp * w.inv_w[c] * phi;
+        out[m] = r.amp * inv_w[c] * phi;
       }
     }
   }
@@ -539,8 +548,7 @@ __global__ void k_spec_eval(long long n, int nc, Ws w) {
 
 template <bool BF16, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict__ cube,
-              int nwmax) {
+k_contract_tc(Geo g, Ws w, int nwmax) {
   constexpr int KSTEPS = KC / 16;
   constexpr int GROUPS = KC / 8;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -559,24 +567,11 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   if (w.hdr->status) return;
   const long long n_items = w.hdr->n_items;
   const int kch = w.hdr->kch;
-  const int dec = w.hdr->edges_dec;
   // Gaussian lines come from the spectrum store when it was filled
   const float* spec = (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 &&
                        w.hdr->spec_ready)
                           ? w.spec
                           : nullptr;
-
-  // exact power-of-two operand scales (FP16 form): largest |W|, |S| -> 2^14
-  float sw = 1.f, ss = 1.f;
-  if (!BF16) {
-    const float wb = __uint_as_float(w.hdr->wbound_bits);
-    const float sb = __uint_as_float(w.hdr->sbound_bits) *
-                     (g.spectral_model == MG_SPECTRUM_TABLE ? 1.f
-                                                            : __uint_as_float(w.hdr->invw_bits));
-    if (wb > 0.f) sw = exp2f(14.f - ceilf(log2f(wb)));
-    if (sb > 0.f) ss = exp2f(14.f - ceilf(log2f(sb)));
-  }
-  const float unscale = 1.f / (sw * ss);
 
   const unsigned a_bytes = KSTEPS * 4096u;
   const unsigned b_bytes = KSTEPS * (unsigned)nwmax * 32u;
@@ -618,7 +613,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
   const int quarter = warp & 3;    // TMEM lane quarter of this warp
   const int colgrp = warp >> 2;    // 4 warps share a quarter: 32-column groups
   const unsigned lane_base = (unsigned)(quarter * 32) << 16;
-  const int ncols = w.seg_width;   // channels of a segment's block held in TMEM (<= 256)
+  int ncols = g.max_width;  // channels of the item's block held in TMEM (<= 256)
 
   const bool drain = ncols <= TC_MASTER_COL;  // master accumulator fits
   auto zero_tmem = [&]() {
@@ -662,6 +657,23 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
     const long long item = s_item;
     if (item >= n_items || s_abort) break;
     const ItemTC it = decode_tc(g, w, item, kch);
+    const Gal& G = w.gal[it.gal];
+    const GalState& gs = w.gst[it.gal];
+    const int dec = gs.dec;
+    const int nc = G.nc;
+    ncols = G.width;
+    // exact power-of-two operand scales of this cube (FP16 form): largest
+    // |W|, |S| -> 2^14
+    float sw = 1.f, ss = 1.f;
+    if (!BF16) {
+      const float wb = __uint_as_float(gs.wbound_bits);
+      const float sb = __uint_as_float(gs.sbound_bits) *
+                       (g.spectral_model == MG_SPECTRUM_TABLE ? 1.f
+                                                              : __uint_as_float(gs.invw_bits));
+      if (wb > 0.f) sw = exp2f(14.f - ceilf(log2f(wb)));
+      if (sb > 0.f) ss = exp2f(14.f - ceilf(log2f(sb)));
+    }
+    const float unscale = 1.f / (sw * ss);
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
     const int nchunk = (it.lcount + KC - 1) / KC;
 
@@ -754,8 +766,9 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
         }
         produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - 2 * (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
                              ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
-        produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, g.nc, dec, g.spectral_model, w.ehi,
-                             w.elo, w.inv_w, spectra, s_pid[buf][q], s_pid[buf][q + 1], lane,
+        produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
+                             w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
+                             (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0), lane,
                              ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf, sb_hi, sb_lo);
       }
       if (has_next && tid < KC) {
@@ -822,17 +835,17 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
     {
       const int p = quarter * 32 + lane;
       const int i = i0 + p / TILE_J, j = j0 + p % TILE_J;
-      const bool inside = i < g.nx && j < g.ny;
+      const bool inside = i < G.nx && j < G.ny;
       float* dst;
       int limit;
       bool vec;
       if (it.nk == 1) {
-        dst = cube + ((long long)i * g.ny + j) * g.nc + it.c0;
-        limit = min(ncols, g.nc - it.c0);
-        vec = (g.nc & 3) == 0 && (limit & 3) == 0;  // 16-byte aligned rows
+        dst = G.cube + ((long long)i * G.ny + j) * nc + it.c0;
+        limit = min(ncols, nc - it.c0);
+        vec = (nc & 3) == 0 && (limit & 3) == 0;  // 16-byte aligned rows
       } else {
         const long long slot = w.part_off[it.seg] + it.kc;
-        dst = w.partial + (slot * TILE_PX + p) * (long long)ncols;
+        dst = w.partial + slot * (long long)(TILE_PX * g.max_width) + (long long)p * ncols;
         limit = ncols;
         vec = true;
       }
@@ -896,8 +909,7 @@ k_contract_tc(Geo g, Ws w, const float* __restrict__ spectra, float* __restrict_
 }
 
 template <bool BF16, int KC>
-int launch_tc(const Geo& g, const Ws& w, const float* spectra, float* cube, int num_sms,
-              cudaStream_t s, int nwmax) {
+int launch_tc(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, int nwmax) {
   constexpr int KSTEPS = KC / 16;
   size_t smem = 2 * (2 * (size_t)KSTEPS * 4096 + 2 * (size_t)KSTEPS * nwmax * 32);
   // at least 116 KB so that one CTA (and its 512 TMEM columns) fits per SM
@@ -912,31 +924,30 @@ int launch_tc(const Geo& g, const Ws& w, const float* spectra, float* cube, int 
       return MG_ERR_CUDA;
   }
   if ((int)smem > attr_bytes) return MG_ERR_UNSUPPORTED;
-  k_contract_tc<BF16, KC><<<num_sms, TC_THREADS, smem, s>>>(g, w, spectra, cube, nwmax);
+  k_contract_tc<BF16, KC><<<num_sms, TC_THREADS, smem, s>>>(g, w, nwmax);
   return MG_OK;
 }
 
 // Spectrum store of the tensor-core forms (Gaussian lines): row lengths,
 // their scan into row offsets, the rows.
-void launch_spec_store(const Geo& g, const Ws& w, long long n, int num_sms, cudaStream_t s) {
+void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
+  const long long n = g.n;
   if (g.spectral_model != MG_SPECTRUM_GAUSSIAN || w.cap_spec <= 0 || n <= 0) return;
   const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, (long long)num_sms * 16);
-  k_spec_count<<<blocks, 256, 0, s>>>(n, w);
+  k_spec_count<<<blocks, 256, 0, s>>>(g, w);
   launch_scan(w.npairs, n, w.pair_off, w.scan_sums, &w.hdr->n_spec, s);
   const unsigned eblocks = (unsigned)std::min<long long>((n + 7) / 8, (long long)num_sms * 16);
-  k_spec_eval<<<eblocks, 256, 0, s>>>(n, g.nc, w);
+  k_spec_eval<<<eblocks, 256, 0, s>>>(g, w);
 }
 
-int launch_contract_bf16x3(const Geo& g, const Ws& w, const float* spectra, float* cube,
-                           int num_sms, cudaStream_t s) {
-  const int nwmax = w.seg_width;  // a stage window never exceeds the segment's block
+int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
+  const int nwmax = g.max_width;  // a stage window never exceeds the widest block
   if (nwmax > TC_MASTER_COL) return MG_ERR_UNSUPPORTED;
   const bool bf16 = g.form == MG_FORM_BF16X3;
-  int rc;
-  rc = bf16 ? launch_tc<true, 64>(g, w, spectra, cube, num_sms, s, nwmax)
-            : launch_tc<false, 64>(g, w, spectra, cube, num_sms, s, nwmax);
+  const int rc = bf16 ? launch_tc<true, 64>(g, w, num_sms, s, nwmax)
+                      : launch_tc<false, 64>(g, w, num_sms, s, nwmax);
   if (rc) return rc;
-  launch_reduce_partials(g, w, cube, num_sms, s);
+  launch_reduce_partials(g, w, num_sms, s);
   return MG_OK;
 }
 

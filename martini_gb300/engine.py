@@ -171,3 +171,86 @@ class InsertionEngine:
         N.check(self.lib.mg_spectra(C.byref(prob), C.c_void_p(out.data_ptr()),
                                     C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
         return out
+
+
+class BatchInsertion:
+    """Many cubes in one insertion (``mg_insert_batched``): one binning pass
+    and one persistent contraction over the tiles of every cube.
+
+    ``probs`` are Problems built with :meth:`InsertionEngine.problem`; the
+    tensors they point to must outlive this object (``keep`` holds them)."""
+
+    def __init__(self, engine: InsertionEngine, probs, keep=None):
+        if not probs:
+            raise ValueError("empty batch")
+        self.eng = engine
+        self.lib = engine.lib
+        self.n = len(probs)
+        self.arr = (N.Problem * self.n)(*probs)
+        self.keep = keep
+        self._ws = None
+        self._caps = (0, 0)
+        self.last_plan = None
+
+    def _stream(self, stream):
+        s = stream or torch.cuda.current_stream(self.eng.device)
+        return C.c_void_p(s.cuda_stream)
+
+    def _workspace(self, nbytes: int) -> torch.Tensor:
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(max(nbytes, 1 << 16), dtype=torch.uint8, device=self.eng.device)
+        return self._ws
+
+    def plan(self, stream=None) -> N.PlanInfo:
+        """Bin every cube and size the workspace (synchronises the stream)."""
+        base = C.c_size_t()
+        N.check(self.lib.mg_workspace_size_batched(self.arr, self.n, 0, 0, C.byref(base)))
+        ws = self._workspace(base.value)
+        info = N.PlanInfo()
+        N.check(self.lib.mg_plan_batched(self.arr, self.n, C.c_void_p(ws.data_ptr()), ws.numel(),
+                                         self._stream(stream), C.byref(info)))
+        self._caps = (int(info.n_pairs), int(info.n_partial_items))
+        self._workspace(int(info.workspace_bytes))
+        self.last_plan = info
+        return info
+
+    def run(self, stream=None) -> None:
+        ws = self._ws
+        N.check(self.lib.mg_insert_batched(self.arr, self.n, C.c_void_p(ws.data_ptr()),
+                                           ws.numel(), self._caps[0], self._caps[1],
+                                           self._stream(stream)))
+
+    def run_stages(self, stages: int, stream=None) -> None:
+        ws = self._ws
+        N.check(self.lib.mg_insert_stages_batched(self.arr, self.n, C.c_void_p(ws.data_ptr()),
+                                                  ws.numel(), self._caps[0], self._caps[1],
+                                                  int(stages), self._stream(stream)))
+
+    def check(self, stream=None) -> None:
+        N.check(self.lib.mg_check(C.c_void_p(self._ws.data_ptr()), self._stream(stream)))
+
+
+def insert_batch(engine: InsertionEngine, items, kernels, spectral_model: int,
+                 form: int = N.MG_FORM_FP32, flux: bool = True):
+    """Insert several cubes in one batch.  ``items``: dicts with ``parts``
+    (DeviceParticles), ``edges`` (device float64), ``nx``, ``ny``, ``nc`` and
+    optionally ``padx``, ``pady``, ``sigma_const``, ``cube``.  Returns a list
+    of (cube, flux) device tensors, one per item."""
+    dev = engine.device
+    probs, outs = [], []
+    for it in items:
+        nx, ny, nc = int(it["nx"]), int(it["ny"]), int(it["nc"])
+        cube = it.get("cube")
+        if cube is None:
+            cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=dev)
+        fl = torch.empty(nc + 1, dtype=torch.float64, device=dev) if flux else None
+        probs.append(engine.problem(it["parts"], kernels, spectral_model,
+                                    float(it.get("sigma_const", 0.0)), nx, ny, nc,
+                                    int(it.get("padx", 0)), int(it.get("pady", 0)), it["edges"],
+                                    cube, fl, form))
+        outs.append((cube, fl))
+    b = BatchInsertion(engine, probs, keep=(items, outs))
+    b.plan()
+    b.run()
+    b.check()
+    return outs

@@ -391,3 +391,47 @@ def test_accumulate_two_spectral_groups(engine, form):
     assert np.abs(got - ref).max() / peak <= FORM_TOL[form]
     tot = ref.sum() + base.astype(np.float64).sum()
     assert abs(flux.cpu().numpy()[0] - tot) / tot <= TOL_FLUX
+
+
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
+def test_batch_of_cubes_matches_oracle(engine, form):
+    """Seven cubes of different shapes, pads and channel grids in one
+    mg_insert_batched call (one binning pass, one contraction queue),
+    including an empty cube and one whose particles all miss it: each cube
+    equals its own oracle insertion."""
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles, insert_batch
+    rng = np.random.default_rng(77)
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    shapes = [(16, 16, 24, 0), (40, 24, 48, 2), (24, 48, 64, 0), (8, 8, 16, 0), (64, 40, 300, 0),
+              (32, 32, 32, 4), (20, 28, 40, 0)]
+    items, refs = [], []
+    for k, (nx, ny, nc, pad) in enumerate(shapes):
+        n = [400, 1500, 2500, 0, 2000, 800, 300][k]
+        h = 10 ** rng.uniform(-0.4, 0.8, n)
+        kidx, size, resc = orc.select_kernels(kernels, h)
+        if k == 6:  # every particle misses the cube
+            x, y = rng.uniform(nx + 40, nx + 60, n), rng.uniform(0, ny, n)
+        else:
+            x, y = rng.normal(nx / 2, nx / 5, n), rng.normal(ny / 2, ny / 5, n)
+        vc = 100.0 + 50 * k
+        edges = orc.vrad_channel_edges(nc, 4.0 if k % 2 == 0 else 3.0, vc)
+        v, sig = rng.normal(vc, 15, n), rng.uniform(3, 9, n)
+        mhi = 10 ** rng.uniform(4, 5, n)
+        spectra = orc.init_spectra("gaussian", mhi, np.full(n, 3.0), v, edges, sig)
+        ranges = orc.sm_ranges(h, size)
+        refs.append(orc.insert_scatter(nx, ny, x, y, ranges, kernels, kidx, h * resc, spectra))
+        parts = DeviceParticles.from_host(engine.device, x, y, ranges, h * resc, kidx, v=v, sigma=sig,
+                                          amp=mhi / 9.0 / orc.MHI_TO_JY)
+        items.append(dict(parts=parts, edges=torch.from_numpy(edges).to(engine.device), nx=nx,
+                          ny=ny, nc=nc, padx=pad, pady=pad))
+    outs = insert_batch(engine, items, native_kernel_table(kernels), N.MG_SPECTRUM_GAUSSIAN,
+                        form=form)
+    for k, ((cube, flux), ref) in enumerate(zip(outs, refs)):
+        got = cube.cpu().numpy().astype(np.float64)
+        pad = shapes[k][3]
+        if np.abs(ref).max() == 0:
+            assert np.abs(got).max() == 0, f"cube {k}"
+            assert flux.cpu().numpy()[0] == 0.0
+            continue
+        assert_close(got, ref, flux.cpu().numpy(), pad=pad, tol=FORM_TOL[form])
