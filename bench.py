@@ -20,6 +20,7 @@ replicas, weak scaling); rank 0 prints the line.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -40,17 +41,23 @@ L2_BYTES = 129 * 1024 * 1024
 TRAFFIC_BYTES = {("disc1m_512", "f16x3"): 3_948_980_480}
 
 
-def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int) -> int:
-    """Kernels one mg_insert launches: tile init, edges, prep, pair scan (3),
-    plan, emit, radix passes x (histogram, scan (3), scatter), segments, item
-    and partial scans (2 x 3), partial check, [spectrum store: row lengths,
-    scan (3), rows], contraction, split-K reduction, flux (2)."""
-    ntiles = ((nx + 7) // 8) * ((ny + 15) // 16)  # 8 x 16-pixel tiles
+def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal: int = 1,
+                      ntiles: int | None = None) -> int:
+    """Kernels one mg_insert(_batched) launches: cube table (one per 16
+    cubes), tile init, edges, prep, pair scan (3), difference-array prefix,
+    tile scan (3), plan, emit, radix passes x (histogram, scan (3), scatter),
+    segments, item and partial scans (2 x 3), partial check, [spectrum store:
+    row lengths, scan (3), rows], [cube clear for batches], contraction,
+    split-K reduction, flux (2)."""
+    if ntiles is None:
+        ntiles = ((nx + 7) // 8) * ((ny + 15) // 16)  # 8 x 16-pixel tiles
     bits = max(ntiles - 1, 0).bit_length() + max(nc - 1, 0).bit_length()
     passes = (bits + 7) // 8
-    n = 1 + 1 + 1 + 3 + 1 + 1 + 5 * passes + 1 + 6 + 1
+    n = (ngal + 15) // 16 + 1 + 1 + 1 + 3 + 1 + 3 + 1 + 1 + 5 * passes + 1 + 6 + 1
     if form != "fp32" and gaussian:
         n += 1 + 3 + 1
+    if ngal > 1:
+        n += 1
     return n + 1 + 1 + 2
 
 
@@ -65,6 +72,8 @@ def parse():
     ap.add_argument("--n", type=int, default=None, help="override particle count")
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-gal", type=int, default=200,
+                    help="galaxies of the disc population (workload disc_population)")
     return ap.parse_args()
 
 
@@ -202,6 +211,11 @@ def main():
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
+    if a.workload == "disc_population":
+        run_population(a, rank, world, local, dev)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     w = workloads.build(a.workload, n=a.n)
     form = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}[a.form]
     edges = torch.from_numpy(np.ascontiguousarray(w["edges"])).to(dev)
@@ -380,19 +394,189 @@ def main():
         dist.destroy_process_group()
 
 
+def run_population(a, rank, world, local, dev):
+    """The disc population as one batch (mg_insert_batched) against the same
+    cubes inserted one call at a time (the looped plain form)."""
+    import torch
+    import torch.distributed as dist
+    from martini_gb300 import _native as N
+    from martini_gb300 import workloads
+    from martini_gb300.engine import BatchInsertion, DeviceParticles, InsertionEngine
+
+    form = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}[a.form]
+    gals = workloads.build_population(a.n_gal, workers=0)
+    eng = InsertionEngine(dev)
+    items, probs = [], []
+    for w in gals:
+        parts = DeviceParticles.from_host(dev, w["x"], w["y"], w["sm_range"], w["h_eff"],
+                                          w["kernel_index"], v=w["v"], sigma=w["sigma"],
+                                          amp=w["amp"])
+        edges = torch.from_numpy(np.ascontiguousarray(w["edges"])).to(dev)
+        cube = torch.empty((w["nx"], w["ny"], w["nc"]), dtype=torch.float32, device=dev)
+        flux = torch.empty(w["nc"] + 1, dtype=torch.float64, device=dev)
+        prob = eng.problem(parts, w["kernels"], w["spectral_model"], w["sigma_const"], w["nx"],
+                           w["ny"], w["nc"], 0, 0, edges, cube, flux, form)
+        items.append(dict(parts=parts, edges=edges, cube=cube, flux=flux, w=w))
+        probs.append(prob)
+    batch = BatchInsertion(eng, probs, keep=items)
+    info = batch.plan()
+    # looped plain form: one mg_insert per cube on one shared workspace
+    loop_eng = InsertionEngine(dev)
+    caps = []
+    for prob in probs:
+        loop_eng.plan(prob)
+        caps.append(loop_eng._caps)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def looped():
+        ws = loop_eng._ws
+        for prob, cp in zip(probs, caps):
+            N.check(loop_eng.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                           cp[0], cp[1], C.c_void_p(stream.cuda_stream)))
+
+    def timed(fn, k):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k)]
+        for s0, e0 in ev:
+            flush.zero_()
+            s0.record(stream)
+            fn()
+            e0.record(stream)
+        torch.cuda.synchronize()
+        return [s0.elapsed_time(e0) / 1e3 for s0, e0 in ev]
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(1.5)
+    for _ in range(a.warmup):
+        flush.zero_()
+        batch.run()
+        looped()
+    torch.cuda.synchronize()
+    batch.check()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_batch = timed(batch.run, a.steps)
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    batch.check()
+    t_loop = timed(looped, a.steps)
+    batch.run_stages(N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
+    t_contract = float(np.mean(timed(lambda: batch.run_stages(N.MG_STAGE_CONTRACT), 3)))
+    # end to end: particles from pinned host memory, every cube back
+    host = []
+    for it in items:
+        w = it["w"]
+        hp = {k: torch.from_numpy(np.ascontiguousarray(w[k], dtype=dt)).pin_memory()
+              for k, dt in (("x", np.float64), ("y", np.float64), ("sm_range", np.float64),
+                            ("h_eff", np.float32), ("v", np.float64), ("amp", np.float64))}
+        if w["kernel_index"] is not None:
+            hp["kernel_index"] = torch.from_numpy(w["kernel_index"].astype(np.int8)).pin_memory()
+        if w["sigma"] is not None:
+            hp["sigma"] = torch.from_numpy(w["sigma"].astype(np.float32)).pin_memory()
+        host.append((hp, {k: getattr(it["parts"], k) for k in hp},
+                     torch.empty(tuple(it["cube"].shape), dtype=torch.float32).pin_memory()))
+    h2d = sum(t.numel() * t.element_size() for hp, _, _ in host for t in hp.values())
+    d2h = sum(hc.numel() * 4 for _, _, hc in host)
+
+    def e2e():
+        for hp, dp, _ in host:
+            for k, t in hp.items():
+                dp[k].copy_(t, non_blocking=True)
+        batch.run()
+        for (_, _, hc), it in zip(host, items):
+            hc.copy_(it["cube"], non_blocking=True)
+
+    e2e()
+    torch.cuda.synchronize()
+    t_e2e = float(np.mean(timed(e2e, max(1, min(a.steps, 3)))))
+    tb, tl = float(np.sum(t_batch)), float(np.sum(t_loop))
+    if world > 1:
+        tt = torch.tensor([tb, tl, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tb, tl, t_e2e = (float(v) for v in tt)
+    if rank != 0:
+        return
+    ng = len(gals)
+    updates = float(sum(workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], w["nx"],
+                                                   w["ny"]).sum() * w["nc"] for w in gals))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak_tf = peaks.get("bf16_tflops", 1900.0)
+    achieved = 2.0 * updates / t_contract / 1e12
+    ntiles = sum(((w["nx"] + 7) // 8) * ((w["ny"] + 15) // 16) for w in gals)
+    line = {
+        "metric": METRIC, "value": world * ng * a.steps / tb, "unit": "cubes/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": tb / a.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": a.form,
+        "data": "synthetic (seeded disc population, no dataset)",
+        "config": {"workload": "disc_population", "galaxies": ng,
+                   "particles": int(sum(w["n"] for w in gals)),
+                   "cubes": "32^2x64 | 64^2x128 | 128^2x128 | 256^2x256 at 4 km/s",
+                   "kernel": "WendlandC2Kernel", "spectrum": "thermal", "form": a.form,
+                   "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"replicas{world}", "pairs": int(info.n_pairs),
+                   "form_batched": True},
+        "looped": {"value": world * ng * a.steps / tl, "unit": "cubes/s",
+                   "ms_per_step": tl / a.steps * 1e3,
+                   "note": "same cubes, one mg_insert per cube"},
+        "particle_channel_updates_per_s": world * updates * a.steps / tb,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf,
+                     "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
+                     "kernel": "k_contract_tc (stage timed: cube clear, contraction, split-K "
+                               "reduction, all cubes)", "contract_ms": t_contract * 1e3,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks
+                     else "fallback 1.9 PFLOP/s"},
+        "e2e": {"value": world * ng / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": a.steps * launches_per_step(a.form, True, 0, 0,
+                                                    max(w["nc"] for w in gals), ng, ntiles),
+        "step_ms": [round(t * 1e3, 3) for t in t_batch],
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(a, rank, world):
     """The reference algorithm (per-pixel numpy restatement) on the host cores."""
     if rank != 0:
         return
     from martini_gb300 import workloads
-    w = workloads.build(a.workload, n=a.n)
     budget = max(2.0, 60.0 / max(1, a.steps + a.warmup))
+    if a.workload == "disc_population":
+        # a seeded sample of the population's galaxies; cubes/s from the mean
+        # time per cube over the sample
+        gals = workloads.build_population(a.n_gal)
+        pick = np.random.default_rng(1).choice(len(gals), min(4, len(gals)), replace=False)
+        sample = [gals[k] for k in pick]
+        w = dict(n=int(sum(g["n"] for g in gals)), nx="32-256", ny="32-256", nc="64-256",
+                 kernel_name="WendlandC2Kernel", spectral_kind="thermal")
+
+        def one(b):
+            tsum = 0.0
+            for g in sample:
+                v, cores, _ = cpu_baseline(g, b / len(sample))
+                tsum += 1.0 / v
+            return len(sample) / tsum, cores, (f"reference per-pixel loop (numpy restatement) on "
+                                               f"{len(sample)} sampled galaxies of {len(gals)}, "
+                                               f"each on a pixel sample, scaled to whole cubes")
+    else:
+        w = workloads.build(a.workload, n=a.n)
+
+        def one(b):
+            return cpu_baseline(w, b)
     for _ in range(a.warmup):
-        cpu_baseline(w, budget / 4)
+        one(budget / 4)
     vals = []
     t0 = time.perf_counter()
     for _ in range(a.steps):
-        v, cores, desc = cpu_baseline(w, budget)
+        v, cores, desc = one(budget)
         vals.append(v)
     wall = time.perf_counter() - t0
     value = float(np.mean(vals))

@@ -19,8 +19,11 @@ Configurations (sizes of the reference workloads being accelerated):
 * ``disc4m_1024``: 4,000,000 particles, R_d 10 kpc at 10 Mpc, h 0.5 kpc
   (0.5 dex); 1024 x 1024 x 512 channels of 2 km/s; WendlandC2, thermal.
 * ``stress16m_2048``: 16,000,000 particles (disc + 10 % of the mass in a
-  Plummer sphere of scale 20 kpc), h log-uniform 0.05-20 kpc, WendlandC2,
-  DiracDeltaSpectrum; 2048 x 2048 x 256.
+  Plummer sphere of scale 20 kpc), h log-uniform 0.05-20 kpc, WendlandC2;
+  thermal Gaussian lines, with a seeded 20 % of the particles on Dirac
+  lines (two spectral groups in one cube); 2048 x 2048 x 256.
+* the disc population (``build_population``): 2000 galaxies of 1e3-1e6
+  particles on cubes of 32^2 x 64 to 256^2 x 256, inserted as one batch.
 """
 
 from __future__ import annotations
@@ -98,9 +101,13 @@ def build(name: str, n: int | None = None):
     edges and the cube shape.  ``n`` overrides the particle count (for
     scaled-down tests of the same configuration).
     """
-    from . import _native as N
     cfg = dict(CONFIGS[name])
     n = cfg["n"] if n is None else int(n)
+    return _assemble(name, cfg, n)
+
+
+def _assemble(name: str, cfg: dict, n: int):
+    from . import _native as N
     g = disc(n, cfg["seed"], **cfg["disc"])
     xyz, vxyz = incline(g["xyz"], g["vxyz"], cfg["incl"])
     if cfg.get("plummer"):
@@ -145,6 +152,51 @@ def build(name: str, n: int | None = None):
         distance=cfg["D"], mHI=src.mHI_g, dist=src.skycoords.distance,
         spectral_kind=kind if groups is None else f"{kind} + {cfg['dirac_fraction']:.0%} dirac",
         kernel_name=cfg["kernel"], native_form_default=N.MG_FORM_FP32)
+
+
+# The disc population: 2000 galaxies, N log-uniform in 1e3-1e6, cos i
+# uniform, v_flat uniform in 50-300 km/s, each on one cube drawn from
+# {32^2 x 64, 64^2 x 128, 128^2 x 128, 256^2 x 256} at 4 km/s; distance,
+# pixel size, kernel and line widths as the single-disc configurations.
+POPULATION = dict(n_gal=2000, seed=4, logn=(3.0, 6.0), v_flat=(50.0, 300.0),
+                  cubes=((32, 64), (64, 128), (128, 128), (256, 256)), D=3.0, dv=4.0, px=10.0,
+                  kernel="WendlandC2Kernel", spectrum=("thermal", None))
+
+
+def population_configs(n_gal: int | None = None, seed: int | None = None):
+    """Per-galaxy configurations of the disc population (one seeded draw
+    order: log N, cos i, v_flat, cube)."""
+    P = POPULATION
+    n_gal = P["n_gal"] if n_gal is None else int(n_gal)
+    seed = P["seed"] if seed is None else int(seed)
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_gal):
+        n = int(round(10 ** rng.uniform(*P["logn"])))
+        incl = float(np.rad2deg(np.arccos(rng.uniform(0.0, 1.0))))
+        vf = float(rng.uniform(*P["v_flat"]))
+        nx, nc = P["cubes"][int(rng.integers(0, len(P["cubes"])))]
+        out.append(dict(n=n, seed=seed * 100003 + k, D=P["D"], incl=incl, nx=nx, nc=nc,
+                        dv=P["dv"], px=P["px"], kernel=P["kernel"], spectrum=P["spectrum"],
+                        disc=dict(v_flat=vf)))
+    return out
+
+
+def _assemble_one(args):
+    k, cfg = args
+    return _assemble(f"pop{k}", cfg, cfg["n"])
+
+
+def build_population(n_gal: int | None = None, seed: int | None = None, workers: int = 0):
+    """The galaxies of the disc population, each as :func:`build` returns it.
+    ``workers`` > 1 builds them in a spawn-started process pool."""
+    cfgs = population_configs(n_gal, seed)
+    jobs = list(enumerate(cfgs))
+    if workers and workers > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            return pool.map(_assemble_one, jobs, chunksize=4)
+    return [_assemble_one(j) for j in jobs]
 
 
 def footprint_pixels(x, y, r, nx, ny):

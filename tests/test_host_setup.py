@@ -170,3 +170,19 @@ def test_kernel_table_of_adaptive_and_single_kernels():
     N.set_kernels(p, rows)
     assert p.n_kernels == 3 and p.kernels[2].type == N.MG_KERNEL_GAUSSIAN
     assert abs(p.kernels[2].truncate - 6.0) < 1e-6
+
+
+def test_population_configs_are_seeded_and_in_range():
+    """The disc population's draws (log N, cos i, v_flat, cube) are fixed by
+    the seed: 2000 galaxies, 288,528,250 particles, every value in range."""
+    from martini_gb300 import workloads as W
+    cf = W.population_configs()
+    assert len(cf) == 2000
+    assert sum(c["n"] for c in cf) == 288_528_250
+    assert all(1000 <= c["n"] <= 1_000_000 for c in cf)
+    assert all(0.0 <= c["incl"] <= 90.0 for c in cf)
+    assert all(50.0 <= c["disc"]["v_flat"] <= 300.0 for c in cf)
+    assert {(c["nx"], c["nc"]) for c in cf} == set(W.POPULATION["cubes"])
+    assert W.population_configs(5) == cf[:5]
+    g = W.build_population(2)
+    assert len(g) == 2 and all(x["n"] > 0 for x in g)
