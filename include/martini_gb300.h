@@ -197,6 +197,72 @@ int mg_insert_stages_batched(const mg_problem* probs, int32_t nprob, void* works
                              int32_t stages, void* stream);
 
 /*
+ * GPU set-up: what Martini.__init__ does on the host before the insertion,
+ * in FP64 on the GPU.  Per particle: sky position, distance and line-of-sight
+ * velocity (martini/sources/sph_source.py:265-326), TAN projection to pixel
+ * coordinates and the spectral pixel (sph_source.py:328-362), smoothing
+ * length in pixels (martini/sph_kernels.py:235-262), adaptive kernel choice,
+ * footprint range (sph_kernels.py:1241-1274, :257-262), amplitude
+ * mHI / D^2 / 2.36e5 and thermal width (spectral_models.py:127-145, :465-485),
+ * then the reference's pruning (martini/martini.py:168-241).  The kept
+ * particles are written in their original order to `out`, ready for
+ * mg_problem.  Asynchronous; the kept count is written to out->n_kept.
+ */
+typedef struct mg_source {
+  int64_t n;
+  const double* xyz;          /* [n][3] kpc, rotation already applied */
+  const double* vxyz;         /* [n][3] km/s */
+  const double* hsm;          /* [n] smoothing lengths, kpc */
+  const double* mHI;          /* [n] Msun */
+  const double* T;            /* [n] K (thermal widths) or NULL */
+  double ra, dec;             /* source position, deg */
+  double distance;            /* Mpc */
+  double vpeculiar;           /* km/s */
+  double h;                   /* Hubble flow h (v = h * 100 km/s/Mpc * r) */
+} mg_source;
+
+typedef struct mg_grid {
+  double crpix[3];            /* 1-based reference pixels (datacube.py:438-486), padded */
+  double cdelt[3];            /* deg, deg, and km/s (VRAD) or Hz (FREQ) */
+  double crval[3];            /* deg, deg, and km/s or Hz */
+  int32_t freq_mode;          /* 1: spectral axis in frequency */
+  int32_t nx, ny, nc;         /* padded spatial sizes, channels */
+  double px_size_arcsec;
+  double max_channel_width;   /* max |dv| of the channel edges, km/s (pruning) */
+} mg_grid;
+
+typedef struct mg_kernel_choice {
+  int32_t n_kernels;          /* 1, or the adaptive tuple's length (<= 4) */
+  int32_t adaptive;           /* 1: index of the first valid kernel, -1 if none */
+  int32_t upper[4];           /* validity: 0: h * rescale >= threshold; 1: <= (DiracDelta) */
+  double threshold[4];
+  double rescale[4];
+  double size_in_fwhm[4];
+} mg_kernel_choice;
+
+#define MG_PRUNE_SPATIAL 1
+#define MG_PRUNE_SPECTRAL 2
+#define MG_PRUNE_MASS 4
+#define MG_PRUNE_ALL 7
+
+typedef struct mg_particles {  /* device arrays with room for n particles */
+  double* x;
+  double* y;
+  double* sm_range;
+  float* h_eff;
+  int8_t* kernel_index;       /* NULL unless adaptive */
+  double* v;                  /* km/s */
+  float* sigma;               /* thermal widths (NULL unless src->T) */
+  double* amp;                /* mHI / D^2 / 2.36e5 */
+  int64_t* n_kept;            /* device scalar */
+} mg_particles;
+
+size_t mg_setup_workspace_size(int64_t n);
+int mg_setup(const mg_source* src, const mg_grid* grid, const mg_kernel_choice* kc,
+             int32_t spectral_model, float sigma_const, int32_t prune, const mg_particles* out,
+             void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Read back the device status word of the last mg_plan/mg_insert on this
  * workspace (SYNCHRONISES the stream).  Returns MG_OK, MG_ERR_WORKSPACE,
  * MG_ERR_NOT_MONOTONIC or MG_ERR_TIMEOUT.

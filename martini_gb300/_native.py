@@ -42,7 +42,7 @@ MG_MAX_KERNELS = 4
 EXPORTS = ("mg_version", "mg_last_error", "mg_workspace_size", "mg_plan", "mg_insert",
            "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux", "mg_insert_noalloc",
            "mg_workspace_size_batched", "mg_plan_batched", "mg_insert_batched",
-           "mg_insert_stages_batched")
+           "mg_insert_stages_batched", "mg_setup_workspace_size", "mg_setup")
 
 MG_NOALLOC_SCRATCH_BYTES = 128 << 20
 
@@ -73,6 +73,37 @@ class Problem(C.Structure):
         ("form", C.c_int32),
         ("accumulate", C.c_int32),
     ]
+
+
+class Source(C.Structure):
+    _fields_ = [("n", C.c_int64), ("xyz", C.c_void_p), ("vxyz", C.c_void_p), ("hsm", C.c_void_p),
+                ("mHI", C.c_void_p), ("T", C.c_void_p), ("ra", C.c_double), ("dec", C.c_double),
+                ("distance", C.c_double), ("vpeculiar", C.c_double), ("h", C.c_double)]
+
+
+class Grid(C.Structure):
+    _fields_ = [("crpix", C.c_double * 3), ("cdelt", C.c_double * 3), ("crval", C.c_double * 3),
+                ("freq_mode", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
+                ("nc", C.c_int32), ("px_size_arcsec", C.c_double),
+                ("max_channel_width", C.c_double)]
+
+
+class KernelChoice(C.Structure):
+    _fields_ = [("n_kernels", C.c_int32), ("adaptive", C.c_int32), ("upper", C.c_int32 * 4),
+                ("threshold", C.c_double * 4), ("rescale", C.c_double * 4),
+                ("size_in_fwhm", C.c_double * 4)]
+
+
+class Particles(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("sm_range", C.c_void_p),
+                ("h_eff", C.c_void_p), ("kernel_index", C.c_void_p), ("v", C.c_void_p),
+                ("sigma", C.c_void_p), ("amp", C.c_void_p), ("n_kept", C.c_void_p)]
+
+
+MG_PRUNE_SPATIAL = 1
+MG_PRUNE_SPECTRAL = 2
+MG_PRUNE_MASS = 4
+MG_PRUNE_ALL = 7
 
 
 class PlanInfo(C.Structure):
@@ -120,11 +151,16 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.mg_insert_stages_batched.argtypes = [P(Problem), C.c_int32, C.c_void_p, C.c_size_t,
                                              C.c_int64, C.c_int64, C.c_int32, C.c_void_p]
     lib.mg_insert_noalloc.argtypes = [P(Problem), C.c_void_p]
+    lib.mg_setup_workspace_size.argtypes = [C.c_int64]
+    lib.mg_setup_workspace_size.restype = C.c_size_t
+    lib.mg_setup.argtypes = [P(Source), P(Grid), P(KernelChoice), C.c_int32, C.c_float, C.c_int32,
+                             P(Particles), C.c_void_p, C.c_size_t, C.c_void_p]
     lib.mg_spectra.argtypes = [P(Problem), C.c_void_p, C.c_void_p]
     lib.mg_flux.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                             C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
     for f in ("mg_workspace_size", "mg_plan", "mg_insert", "mg_insert_stages", "mg_check",
-              "mg_spectra", "mg_flux", "mg_insert_noalloc"):
+              "mg_spectra", "mg_flux", "mg_insert_noalloc", "mg_workspace_size_batched",
+              "mg_plan_batched", "mg_insert_batched", "mg_insert_stages_batched", "mg_setup"):
         getattr(lib, f).restype = C.c_int
     _lib = lib
     return lib

@@ -254,3 +254,86 @@ def insert_batch(engine: InsertionEngine, items, kernels, spectral_model: int,
     b.run()
     b.check()
     return outs
+
+
+def kernel_choice(sph_kernel) -> N.KernelChoice:
+    """Validity rules and constants of an SPH kernel (adaptive tuple or single
+    kernel) for the GPU kernel choice (sph_kernels.py:1241-1274)."""
+    kc = N.KernelChoice()
+    subs = getattr(sph_kernel, "kernels", None)
+    kc.adaptive = 1 if subs else 0
+    subs = subs or (sph_kernel,)
+    kc.n_kernels = len(subs)
+    for k, K in enumerate(subs):
+        upper = hasattr(K, "max_valid_size")
+        kc.upper[k] = 1 if upper else 0
+        kc.threshold[k] = float(K.max_valid_size if upper else K.min_valid_size)
+        kc.rescale[k] = float(K._rescale)
+        kc.size_in_fwhm[k] = float(K.size_in_fwhm)
+    return kc
+
+
+def setup_on_gpu(engine: InsertionEngine, source, datacube, sph_kernel, spectral_model,
+                 prune: int = N.MG_PRUNE_ALL):
+    """``Martini.__init__``'s set-up on the GPU in FP64 (mg_setup): sky
+    coordinates, pixel coordinates, smoothing lengths, kernel choice, ranges,
+    amplitudes, thermal widths and pruning, from the source's rotated
+    particle arrays.  Returns (DeviceParticles of the kept particles, kernel
+    table, spectral model code, constant sigma)."""
+    dev = engine.device
+
+    def put(a, dt):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
+
+    n = int(source.npart)
+    xyz, vxyz = put(source.xyz_g, np.float64), put(source.vxyz_g, np.float64)
+    hsm = put(source.hsm_g, np.float64)
+    mhi = put(source.mHI_g, np.float64)
+    model = spectral_model.native_model
+    thermal = getattr(spectral_model, "sigma_mode", None) == "thermal"
+    T = put(np.broadcast_to(source.T_g, (n,)), np.float64) if thermal else None
+    sigma_const = 0.0
+    if model == N.MG_SPECTRUM_GAUSSIAN and not thermal:
+        sigma_const = float(spectral_model.sigma_mode)
+    src = N.Source()
+    src.n = n
+    src.xyz, src.vxyz, src.hsm, src.mHI = (_ptr(t) for t in (xyz, vxyz, hsm, mhi))
+    src.T = _ptr(T)
+    src.ra, src.dec = float(source.ra), float(source.dec)
+    src.distance, src.vpeculiar, src.h = (float(source.distance), float(source.vpeculiar),
+                                          float(source.h))
+    gr = N.Grid()
+    for k in range(3):
+        gr.crpix[k], gr.cdelt[k], gr.crval[k] = (float(datacube.crpix[k]),
+                                                 float(datacube.cdelt[k]),
+                                                 float(datacube.crval[k]))
+    gr.freq_mode = 1 if datacube._freq_channel_mode else 0
+    gr.nx, gr.ny = (int(v) for v in datacube._array.shape[:2])
+    gr.nc = int(datacube.n_channels)
+    gr.px_size_arcsec = float(datacube.px_size)
+    gr.max_channel_width = float(np.max(np.abs(np.diff(datacube.velocity_channel_edges))))
+    kc = kernel_choice(sph_kernel)
+    out_t = dict(x=torch.empty(n, dtype=torch.float64, device=dev),
+                 y=torch.empty(n, dtype=torch.float64, device=dev),
+                 sm_range=torch.empty(n, dtype=torch.float64, device=dev),
+                 h_eff=torch.empty(n, dtype=torch.float32, device=dev),
+                 kernel_index=torch.empty(n, dtype=torch.int8, device=dev) if kc.adaptive
+                 else None,
+                 v=torch.empty(n, dtype=torch.float64, device=dev),
+                 sigma=torch.empty(n, dtype=torch.float32, device=dev) if thermal else None,
+                 amp=torch.empty(n, dtype=torch.float64, device=dev))
+    n_kept = torch.zeros(1, dtype=torch.int64, device=dev)
+    out = N.Particles()
+    for k, t in out_t.items():
+        setattr(out, k, _ptr(t))
+    out.n_kept = _ptr(n_kept)
+    ws = torch.empty(int(engine.lib.mg_setup_workspace_size(n)), dtype=torch.uint8, device=dev)
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    N.check(engine.lib.mg_setup(C.byref(src), C.byref(gr), C.byref(kc), int(model),
+                                float(sigma_const), int(prune), C.byref(out),
+                                C.c_void_p(ws.data_ptr()), ws.numel(), s))
+    m = int(n_kept.item())
+    cut = {k: (None if t is None else t[:m]) for k, t in out_t.items()}
+    parts = DeviceParticles(cut["x"], cut["y"], cut["sm_range"], cut["h_eff"],
+                            cut["kernel_index"], v=cut["v"], sigma=cut["sigma"], amp=cut["amp"])
+    return parts, sph_kernel._device_kernels(), model, sigma_const
