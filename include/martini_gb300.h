@@ -263,6 +263,32 @@ int mg_setup(const mg_source* src, const mg_grid* grid, const mg_kernel_choice* 
              void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * Global profile: the spatially integrated spectrum of a source, in Jy
+ * (GlobalProfile.insert_source_in_spectrum, martini/martini.py:1551-1596:
+ * every particle that survives spectral and mass pruning contributes its
+ * whole line).  Uses p->n, v, sigma / sigma_const, amp, spectral_model (GAUSSIAN
+ * or DIRAC), nc and edges; the spatial fields are ignored.  spectrum[nc] is
+ * FP64 on the device.  Deterministic (fixed summation order).  Asynchronous;
+ * mg_check(workspace) reports non-monotonic channel edges.
+ */
+size_t mg_global_profile_workspace_size(int64_t n, int32_t nc);
+int mg_global_profile(const mg_problem* p, double* spectrum, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/*
+ * Beam convolution (Martini.convolve_beam, martini/martini.py:863-901):
+ * out = scale * (cube (*) kernel) in "same" mode per channel (the reference's
+ * scipy fftconvolve of each spatial slice), over the unpadded pixels only,
+ * with zeros outside the padded cube.  cube: device [nx][ny][nc] (padded),
+ * kernel: device [kx][ky] (odd sizes, pads >= half sizes), out: device
+ * [nx - 2 padx][ny - 2 pady][nc].  scale converts Jy/arcsec^2 to Jy/beam
+ * (the beam area in arcsec^2).  FP32 accumulation.  Asynchronous.
+ */
+int mg_convolve_beam(const float* cube, int32_t nx, int32_t ny, int32_t nc, int32_t padx,
+                     int32_t pady, const float* kernel, int32_t kx, int32_t ky, float scale,
+                     float* out, void* stream);
+
+/*
  * Read back the device status word of the last mg_plan/mg_insert on this
  * workspace (SYNCHRONISES the stream).  Returns MG_OK, MG_ERR_WORKSPACE,
  * MG_ERR_NOT_MONOTONIC or MG_ERR_TIMEOUT.

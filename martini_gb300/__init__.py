@@ -6,10 +6,10 @@ fallback).
 """
 
 from .datacube import DataCube
-from .martini import Martini
+from .martini import GlobalProfile, Martini
 from .sources import SPHSource
 from . import sph_kernels, spectral_models
 
 __version__ = "0.1.0"
 
-__all__ = ["Martini", "DataCube", "SPHSource", "sph_kernels", "spectral_models", "__version__"]
+__all__ = ["Martini", "GlobalProfile", "DataCube", "SPHSource", "sph_kernels", "spectral_models", "__version__"]

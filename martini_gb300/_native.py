@@ -42,7 +42,8 @@ MG_MAX_KERNELS = 4
 EXPORTS = ("mg_version", "mg_last_error", "mg_workspace_size", "mg_plan", "mg_insert",
            "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux", "mg_insert_noalloc",
            "mg_workspace_size_batched", "mg_plan_batched", "mg_insert_batched",
-           "mg_insert_stages_batched", "mg_setup_workspace_size", "mg_setup")
+           "mg_insert_stages_batched", "mg_setup_workspace_size", "mg_setup",
+           "mg_global_profile_workspace_size", "mg_global_profile", "mg_convolve_beam")
 
 MG_NOALLOC_SCRATCH_BYTES = 128 << 20
 
@@ -151,6 +152,12 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.mg_insert_stages_batched.argtypes = [P(Problem), C.c_int32, C.c_void_p, C.c_size_t,
                                              C.c_int64, C.c_int64, C.c_int32, C.c_void_p]
     lib.mg_insert_noalloc.argtypes = [P(Problem), C.c_void_p]
+    lib.mg_global_profile_workspace_size.argtypes = [C.c_int64, C.c_int32]
+    lib.mg_global_profile_workspace_size.restype = C.c_size_t
+    lib.mg_global_profile.argtypes = [P(Problem), C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.mg_convolve_beam.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                     C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_float,
+                                     C.c_void_p, C.c_void_p]
     lib.mg_setup_workspace_size.argtypes = [C.c_int64]
     lib.mg_setup_workspace_size.restype = C.c_size_t
     lib.mg_setup.argtypes = [P(Source), P(Grid), P(KernelChoice), C.c_int32, C.c_float, C.c_int32,
@@ -160,7 +167,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                             C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
     for f in ("mg_workspace_size", "mg_plan", "mg_insert", "mg_insert_stages", "mg_check",
               "mg_spectra", "mg_flux", "mg_insert_noalloc", "mg_workspace_size_batched",
-              "mg_plan_batched", "mg_insert_batched", "mg_insert_stages_batched", "mg_setup"):
+              "mg_plan_batched", "mg_insert_batched", "mg_insert_stages_batched", "mg_setup",
+              "mg_global_profile", "mg_convolve_beam"):
         getattr(lib, f).restype = C.c_int
     _lib = lib
     return lib

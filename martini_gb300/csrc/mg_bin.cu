@@ -12,69 +12,6 @@
 
 namespace mg {
 
-// Inclusive pixel range [lo, hi] of {i : |i - c| <= r}, clipped to [0, n).
-__device__ __forceinline__ void box_bounds(double c, double r, int n, int& lo, int& hi) {
-  if (!(r >= 0.0)) {  // NaN or negative range: empty
-    lo = 0;
-    hi = -1;
-    return;
-  }
-  if (isinf(r)) {
-    lo = 0;
-    hi = n - 1;
-    return;
-  }
-  double a = floor(c - r) - 1.0;
-  double b = ceil(c + r) + 1.0;
-  if (a < 0.0) a = 0.0;
-  if (b > (double)(n - 1)) b = (double)(n - 1);
-  if (a > b) {
-    lo = 0;
-    hi = -1;
-    return;
-  }
-  int l = (int)a, h = (int)b;
-  while (l <= h && !(fabs((double)l - c) <= r)) ++l;
-  while (h >= l && !(fabs((double)h - c) <= r)) --h;
-  lo = l;
-  hi = h;
-}
-
-// Channel index range whose closed velocity interval meets [lo, hi].
-__device__ __forceinline__ void channel_range(const double* e, int nc, int dec, double lo,
-                                              double hi, int& c0, int& c1) {
-  // E(k) = edges in increasing order
-  auto E = [&](int k) { return dec ? e[nc - k] : e[k]; };
-  // first c in [0, nc) with E(c + 1) >= lo
-  int a = 0, b = nc;
-  while (a < b) {
-    int m = (a + b) >> 1;
-    if (E(m + 1) >= lo) b = m; else a = m + 1;
-  }
-  int first = a;
-  // last c in [0, nc) with E(c) <= hi  ->  (first c with E(c) > hi) - 1
-  a = 0;
-  b = nc;
-  while (a < b) {
-    int m = (a + b) >> 1;
-    if (E(m) > hi) b = m; else a = m + 1;
-  }
-  int last = a - 1;
-  if (first > last) {
-    c0 = 1;
-    c1 = 0;
-    return;
-  }
-  if (dec) {
-    c0 = nc - 1 - last;
-    c1 = nc - 1 - first;
-  } else {
-    c0 = first;
-    c1 = last;
-  }
-}
-
-
 // ---------------------------------------------------------------------------
 // The galaxy table: kernel parameters into the workspace (no host copy, so
 // the insertion can be captured in a CUDA graph).

@@ -337,3 +337,37 @@ def setup_on_gpu(engine: InsertionEngine, source, datacube, sph_kernel, spectral
     parts = DeviceParticles(cut["x"], cut["y"], cut["sm_range"], cut["h_eff"],
                             cut["kernel_index"], v=cut["v"], sigma=cut["sigma"], amp=cut["amp"])
     return parts, sph_kernel._device_kernels(), model, sigma_const
+
+
+def global_profile(engine: InsertionEngine, parts: DeviceParticles, spectral_model: int,
+                   sigma_const: float, nc: int, edges: torch.Tensor) -> torch.Tensor:
+    """Spatially integrated spectrum (Jy, FP64 on the device) of the
+    particles' lines: mg_global_profile (martini/martini.py:1551-1596)."""
+    dev = engine.device
+    out = torch.empty(nc, dtype=torch.float64, device=dev)
+    dummy = torch.empty(1, dtype=torch.float32, device=dev)
+    prob = engine.problem(parts, [(N.MG_KERNEL_DIRAC, 0.0)], spectral_model, sigma_const, 1, 1,
+                          nc, 0, 0, edges, dummy, None, N.MG_FORM_FP32)
+    ws = torch.empty(int(engine.lib.mg_global_profile_workspace_size(parts.n, nc)),
+                     dtype=torch.uint8, device=dev)
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    N.check(engine.lib.mg_global_profile(C.byref(prob), C.c_void_p(out.data_ptr()),
+                                         C.c_void_p(ws.data_ptr()), ws.numel(), s))
+    N.check(engine.lib.mg_check(C.c_void_p(ws.data_ptr()), s))
+    return out
+
+
+def convolve_beam(engine: InsertionEngine, cube: torch.Tensor, padx: int, pady: int,
+                  kernel: np.ndarray, scale: float) -> torch.Tensor:
+    """Beam convolution of a padded device cube (mg_convolve_beam); returns the
+    unpadded float32 cube times ``scale``."""
+    dev = engine.device
+    nx, ny, nc = (int(v) for v in cube.shape)
+    k = torch.from_numpy(np.ascontiguousarray(kernel, dtype=np.float32)).to(dev)
+    out = torch.empty((nx - 2 * padx, ny - 2 * pady, nc), dtype=torch.float32, device=dev)
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    N.check(engine.lib.mg_convolve_beam(C.c_void_p(cube.data_ptr()), nx, ny, nc, int(padx),
+                                        int(pady), C.c_void_p(k.data_ptr()), int(k.shape[0]),
+                                        int(k.shape[1]), float(scale),
+                                        C.c_void_p(out.data_ptr()), s))
+    return out

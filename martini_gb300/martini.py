@@ -190,3 +190,207 @@ class Martini(_BaseMartini):
         (martini/martini.py:827-861)."""
         super()._insert_source_in_cube(skip_validation=skip_validation, progressbar=progressbar,
                                        ncpu=ncpu)
+
+    def _wcs_cards(self):
+        """Axis cards of the cube's WCS (datacube.py:438-486): RA---TAN and
+        DEC--TAN in deg, VRAD in m/s or FREQ in Hz."""
+        dc = self._datacube
+        freq = dc._freq_channel_mode
+        cards = [("CDELT1", -dc.px_size / 3600.0), ("CRPIX1", dc.n_px_x / 2.0 + 0.5 + dc.padx),
+                 ("CRVAL1", float(dc.ra)), ("CTYPE1", "RA---TAN"), ("CUNIT1", "deg"),
+                 ("CDELT2", dc.px_size / 3600.0), ("CRPIX2", dc.n_px_y / 2.0 + 0.5 + dc.pady),
+                 ("CRVAL2", float(dc.dec)), ("CTYPE2", "DEC--TAN"), ("CUNIT2", "deg"),
+                 ("CDELT3", abs(dc.channel_width) if freq else -abs(dc.channel_width) * 1e3),
+                 ("CRPIX3", dc.n_channels / 2.0 + 0.5),
+                 ("CRVAL3", float(dc.spectral_centre) * (1.0 if freq else 1e3)),
+                 ("CTYPE3", "FREQ" if freq else "VRAD"), ("CUNIT3", "Hz" if freq else "m/s")]
+        return cards
+
+    def write_fits(self, filename: str, overwrite: bool = True, obj_name: str = "MOCK",
+                   channels=None, dtype=None):
+        """Write the cube to a FITS file (martini/martini.py:939-1051): the pad is
+        dropped, '.fits' appended if absent, the reference's header cards."""
+        import time as _time
+        from . import __version__
+        from .fits import write_primary
+        dc = self._datacube
+        dc.drop_pad()
+        filename = filename + ".fits" if "fits" not in filename.split(".") else filename
+        arr = dc._array
+        unit = {"Jy/pix2": "Jy pix-2", "Jy/arcsec2": "Jy arcsec-2", "Jy/beam": "Jy/beam"}.get(
+            dc._array_unit, dc._array_unit)
+        cards = [("EXTEND", True)] + self._wcs_cards()
+        if dc.stokes_axis:
+            cards += [("CDELT4", 1.0), ("CRPIX4", 1.0), ("CRVAL4", 1.0), ("CTYPE4", "STOKES"),
+                      ("CUNIT4", "PAR")]
+        now = _time.time()
+        mjd = now / 86400.0 + 40587.0
+        cards += [("EPOCH", 2000), ("INSTRUME", "MARTINI", f"martini_gb300 {__version__}"),
+                  ("BSCALE", 1.0), ("BZERO", 0.0), ("DATAMAX", float(np.max(arr))),
+                  ("DATAMIN", float(np.min(arr))), ("ORIGIN", "martini_gb300"),
+                  ("OBJECT", obj_name[:16])]
+        if self.beam is not None:
+            cards.append(("BPA", float(self.beam.bpa)))
+        cards += [("OBSERVER", "K. Oman"), ("BUNIT", unit),
+                  ("DATE-OBS", _time.strftime("%Y-%m-%dT%H:%M:%S", _time.gmtime(now))),
+                  ("MJD-OBS", mjd)]
+        if self.beam is not None:
+            cards += [("BMAJ", self.beam.bmaj / 3600.0), ("BMIN", self.beam.bmin / 3600.0)]
+        cards += [("BTYPE", "Intensity"), ("SPECSYS", "ICRS"), ("RESTFRQ", 1420405751.768)]
+        data = arr.T
+        if dtype is not None:
+            data = data.astype(dtype, copy=False)
+        write_primary(filename, cards, data, overwrite=overwrite)
+
+    def write_beam_fits(self, filename: str, overwrite: bool = True, channels=None):
+        """Write the beam image to a FITS file (martini/martini.py:1053-1105)."""
+        from . import __version__
+        from .fits import write_primary
+        if self.beam is None:
+            raise ValueError("Martini.write_beam_fits: Called with beam set to 'None'.")
+        filename = filename if filename[-5:] == ".fits" else filename + ".fits"
+        k = np.asarray(self.beam.kernel, dtype=np.float64)
+        w = dict((c[0], c[1]) for c in self._wcs_cards())
+        cards = [("EXTEND", True), ("BSCALE", 1.0), ("BZERO", 0.0), ("BUNIT", ""),
+                 ("CRPIX1", k.shape[0] // 2 + 1), ("CDELT1", w["CDELT1"]), ("CRVAL1", w["CRVAL1"]),
+                 ("CTYPE1", w["CTYPE1"]), ("CUNIT1", w["CUNIT1"]),
+                 ("CRPIX2", k.shape[1] // 2 + 1), ("CDELT2", w["CDELT2"]), ("CRVAL2", w["CRVAL2"]),
+                 ("CTYPE2", w["CTYPE2"]), ("CUNIT2", w["CUNIT2"]),
+                 ("CRPIX3", 1), ("CDELT3", w["CDELT3"]), ("CRVAL3", w["CRVAL3"]),
+                 ("CTYPE3", w["CTYPE3"]), ("CUNIT3", w["CUNIT3"]), ("SPECSYS", "ICRS"),
+                 ("BMAJ", self.beam.bmaj / 3600.0), ("BMIN", self.beam.bmin / 3600.0),
+                 ("BPA", float(self.beam.bpa)), ("BTYPE", "beam"), ("EPOCH", 2000),
+                 ("OBSERVER", "K. Oman"), ("OBJECT", "MOCKBEAM"),
+                 ("INSTRUME", "MARTINI", f"martini_gb300 {__version__}"),
+                 ("DATAMAX", float(k.max())), ("DATAMIN", float(k.min())),
+                 ("ORIGIN", "martini_gb300")]
+        write_primary(filename, cards, k[np.newaxis, ...].transpose(0, 2, 1),
+                      overwrite=overwrite)
+
+    def convolve_beam(self):
+        """Convolve the cube with the beam on the GPU, drop the pad and convert
+        to Jy/beam (martini/martini.py:863-901)."""
+        import warnings
+
+        import torch
+        from .engine import convolve_beam
+        if self.beam is None:
+            warnings.warn("Skipping beam convolution, no beam object provided to Martini.")
+            return
+        dc = self._datacube
+        px, py = self.beam.needs_pad()
+        if dc.padx < px or dc.pady < py:
+            raise ValueError("datacube padding insufficient for beam convolution (perhaps you "
+                             "loaded a datacube state with datacube.load_state that was "
+                             "previously initialized by martini with a smaller beam?)")
+        arr = dc._array[..., 0] if dc.stokes_axis else dc._array
+        if dc._array_unit == "Jy/pix2":
+            arr = arr / dc.px_size ** 2
+        cube = torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float32)).to(
+            self.engine.device)
+        out = convolve_beam(self.engine, cube, dc.padx, dc.pady, self.beam.kernel,
+                            self.beam.area).cpu().numpy().astype(np.float64)
+        dc._array = out[..., np.newaxis] if dc.stokes_axis else out
+        dc.padx, dc.pady = 0, 0
+        dc._array_unit = "Jy/beam"
+        if not self.quiet:
+            a = dc._array
+            pos = a[a > 0]
+            print("Beam convolved.",
+                  f"  Data cube RMS after beam convolution: {np.std(a):.2e} Jy / beam",
+                  f"  Maximum pixel: {a.max():.2e} Jy / beam",
+                  "  Median non-zero pixel: "
+                  f"{(np.median(pos) if pos.size else 0.0):.2e} Jy / beam", sep="\n")
+
+
+class GlobalProfile(_BaseMartini):
+    """The spatially integrated spectrum of a source, on the GPU
+    (martini/martini.py:1369-1738).
+
+    Every particle contributes its whole line unless it falls outside the
+    band (spectral and mass pruning only, no spatial aperture); positions
+    still set each particle's line of sight.  Same constructor as the
+    reference; ``spectrum`` is in Jy.
+    """
+
+    def __init__(self, *, source, spectral_model, n_channels: int, channel_width,
+                 spectral_centre=0.0, quiet: bool = False, channels=None, device=None):
+        from .sph_kernels import DiracDeltaKernel
+        datacube = DataCube(n_px_x=1, n_px_y=1, n_channels=n_channels, px_size=3600.0,
+                            channel_width=channel_width, spectral_centre=spectral_centre)
+        super().__init__(source=source, datacube=datacube, beam=None, noise=None,
+                         sph_kernel=DiracDeltaKernel(size_in_fwhm=np.inf),
+                         spectral_model=spectral_model, quiet=quiet,
+                         _prune_kwargs=dict(spatial=False, spectral=True, mass=True,
+                                            obj_type_str="spectrum"),
+                         form="fp32", device=device)
+        self.source.pixcoords[:2] = 0
+
+    def insert_source_in_spectrum(self):
+        """Form the spectrum (martini/martini.py:1551-1596): sum of the lines of
+        every particle in the band, in Jy; the one-pixel cube holds it in
+        Jy/arcsec^2 as the reference's does."""
+        import torch
+        from .engine import DeviceParticles, global_profile
+        if self.spectral_model._owner is not self:
+            self.init_spectra()
+        src, dc, sm = self.source, self._datacube, self.spectral_model
+        sig, sig_const = sm._device_sigma(src)
+        amp = src.mHI_g * np.power(src.skycoords.distance, -2.0) / MHI_TO_JY
+        n = src.npart
+        zeros = np.zeros(n)
+        dev = self.engine.device
+        parts = DeviceParticles.from_host(dev, zeros, zeros, zeros, zeros.astype(np.float32),
+                                          v=src.skycoords.radial_velocity, sigma=sig, amp=amp)
+        edges = torch.from_numpy(np.ascontiguousarray(dc.velocity_channel_edges,
+                                                      dtype=np.float64)).to(dev)
+        spec = global_profile(self.engine, parts, sm.native_model, sig_const, dc.n_channels,
+                              edges).cpu().numpy()
+        self._spectrum = spec
+        px2 = dc.px_size ** 2
+        add = (spec / px2).reshape(1, 1, -1)
+        if dc.stokes_axis:
+            add = add[..., np.newaxis]
+        if dc._array_unit == "Jy/pix2":
+            dc._array = dc._array / px2
+        dc._array = dc._array + add
+        dc._array_unit = "Jy/arcsec2"
+        if not self.quiet:
+            flux = float(spec.sum())
+            mass = MHI_TO_JY * src.distance ** 2 * flux * dc.channel_width
+            print("Source inserted.",
+                  f"  Flux density in spectrum: {flux:.2e} Jy",
+                  f"  Mass in spectrum (assuming distance {src.distance:.2f} Mpc): {mass:.2e} "
+                  "solMass",
+                  f"    [{mass / src.input_mass * 100:.0f}% of initial source mass]", sep="\n")
+
+    @property
+    def spectrum(self):
+        """Spatially integrated spectrum (Jy), formed on first access."""
+        if not hasattr(self, "_spectrum"):
+            self.insert_source_in_spectrum()
+        return self._spectrum
+
+    @property
+    def channel_edges(self):
+        return self._datacube.channel_edges
+
+    @property
+    def channel_mids(self):
+        return self._datacube.channel_mids
+
+    @property
+    def frequency_channel_edges(self):
+        return self._datacube.frequency_channel_edges
+
+    @property
+    def frequency_channel_mids(self):
+        return self._datacube.frequency_channel_mids
+
+    @property
+    def velocity_channel_edges(self):
+        return self._datacube.velocity_channel_edges
+
+    @property
+    def velocity_channel_mids(self):
+        return self._datacube.velocity_channel_mids
