@@ -109,9 +109,12 @@ k_contract_fp32(Geo g, Ws w) {
         const int q = tid >> 3, ii = tid & 7;
         const PRec r = recs[q];
         const int i = i0 + ii;
+        // a particle listed for this block whose line misses it (the list
+        // bound is conservative) contributes nothing: no weights
+        const bool hit = r.chi >= it.c0 && r.clo < it.c0 + CBLK;
 #pragma unroll 4
         for (int jj = 0; jj < TILE_J; ++jj)
-          Ws_[q][ii * TILE_J + jj] = pixel_weight(r, s_ks, i, j0 + jj);
+          Ws_[q][ii * TILE_J + jj] = hit ? pixel_weight(r, s_ks, i, j0 + jj) : 0.f;
         // S: particle q, channels c0 + ii*8 .. +7
         for (int cc = ii * 8; cc < ii * 8 + 8; ++cc) {
           const int c = it.c0 + cc;

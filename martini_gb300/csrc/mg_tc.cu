@@ -413,8 +413,9 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
                                                const float* inv_w, const float* spectra,
                                                int pid0, int pid1, int lane, float ss,
                                                const float* spec, long long soff0,
-                                               long long soff1, const float (&pf)[4],
-                                               unsigned char* b_hi, unsigned char* b_lo) {
+                                               long long soff1, float pf0, float pf1,
+                                               float pf2, float pf3, unsigned char* b_hi,
+                                               unsigned char* b_lo) {
   const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
                         (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
   if (spec) {
@@ -425,11 +426,11 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
       const int c = w0 + n;
       float s0, s1;
       if (base == 0) {
-        s0 = pf[0];
-        s1 = pf[1];
+        s0 = pf0;
+        s1 = pf1;
       } else if (base == 32) {
-        s0 = pf[2];
-        s1 = pf[3];
+        s0 = pf2;
+        s1 = pf3;
       } else {
         s0 = spec_at(spec, soff0, r0, v0, c);
         s1 = spec_at(spec, soff1, r1, v1, c);
@@ -646,8 +647,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   tc_fence_before();
   __syncthreads();
 
-  unsigned phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
+  // per stage buffer s: bit s of phase_bits is its mbarrier parity, bit s
+  // of pending_bits says MMAs reading it are in flight (registers, not a
+  // dynamically indexed array)
+  unsigned phase_bits = 0u, pending_bits = 0u;
   int stage = 0;
   int since_drain = 0;
 
@@ -697,10 +700,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       const int k0 = ch * KC;
       const int kn = min(KC, it.lcount - k0);
       // the stage must be free: every thread waits for the MMAs that last read it
-      if (pending[stage]) {
-        if (!mbar_wait(smem_u32(&bars[stage]), phase[stage])) s_abort = 1;
-        phase[stage] ^= 1u;
-        pending[stage] = false;
+      if ((pending_bits >> stage) & 1u) {
+        if (!mbar_wait(smem_u32(&bars[stage]), (phase_bits >> stage) & 1u)) s_abort = 1;
+        phase_bits ^= 1u << stage;
+        pending_bits &= ~(1u << stage);
       }
       // fetch the next stage's records while this one is produced
       PRec nrec;
@@ -752,24 +755,29 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         const int q = warp * PPW + pp;
         const PRec r0 = recs[buf][q];
         const PRec r1 = recs[buf][q + 1];
-        const bool v0 = q < kn, v1 = q + 1 < kn;
+        // a particle listed for this block whose line misses the block (the
+        // list bound is conservative) contributes nothing: no weights
+        const int cb0 = it.c0, cb1 = it.c0 + ncols - 1;
+        const bool v0 = q < kn && r0.chi >= cb0 && r0.clo <= cb1;
+        const bool v1 = q + 1 < kn && r1.chi >= cb0 && r1.clo <= cb1;
         // spectrum store loads of the first 64 window channels, in flight
         // while the weights are computed
-        float pf[4] = {0.f, 0.f, 0.f, 0.f};
+        float pf0 = 0.f, pf1 = 0.f, pf2 = 0.f, pf3 = 0.f;
         if (spec) {
           const long long so0 = s_soff[buf][q], so1 = s_soff[buf][q + 1];
           const int wa = it.c0 + w0;
-          pf[0] = spec_at(spec, so0, r0, v0, wa + lane);
-          pf[1] = spec_at(spec, so1, r1, v1, wa + lane);
-          pf[2] = spec_at(spec, so0, r0, v0, wa + 32 + lane);
-          pf[3] = spec_at(spec, so1, r1, v1, wa + 32 + lane);
+          pf0 = spec_at(spec, so0, r0, v0, wa + lane);
+          pf1 = spec_at(spec, so1, r1, v1, wa + lane);
+          pf2 = spec_at(spec, so0, r0, v0, wa + 32 + lane);
+          pf3 = spec_at(spec, so1, r1, v1, wa + 32 + lane);
         }
         produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - 2 * (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
                              ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
         produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
                              w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
                              (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0), lane,
-                             ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf, sb_hi, sb_lo);
+                             ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf0, pf1, pf2, pf3, sb_hi,
+                             sb_lo);
       }
       if (has_next && tid < KC) {
         recs[buf ^ 1][tid] = nrec;
@@ -799,14 +807,14 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         }
         umma_commit(smem_u32(&bars[stage]));
       }
-      pending[stage] = true;
+      pending_bits |= 1u << stage;
       stage ^= 1;
       if (drain && ++since_drain == TC_DRAIN && ch + 1 < nchunk) {
         // wait for this stage's MMAs (the commit covers all earlier ones)
         const int s = stage ^ 1;
-        if (!mbar_wait(smem_u32(&bars[s]), phase[s])) s_abort = 1;
-        phase[s] ^= 1u;
-        pending[s] = false;
+        if (!mbar_wait(smem_u32(&bars[s]), (phase_bits >> s) & 1u)) s_abort = 1;
+        phase_bits ^= 1u << s;
+        pending_bits &= ~(1u << s);
         tc_fence_after();
         drain_tmem();
         tc_fence_before();
@@ -819,10 +827,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
 
     // all MMAs of the item complete (a commit covers every earlier MMA)
     for (int s = 0; s < 2; ++s) {
-      if (pending[s]) {
-        if (!mbar_wait(smem_u32(&bars[s]), phase[s])) s_abort = 1;
-        phase[s] ^= 1u;
-        pending[s] = false;
+      if ((pending_bits >> s) & 1u) {
+        if (!mbar_wait(smem_u32(&bars[s]), (phase_bits >> s) & 1u)) s_abort = 1;
+        phase_bits ^= 1u << s;
+        pending_bits &= ~(1u << s);
       }
     }
     __syncthreads();
