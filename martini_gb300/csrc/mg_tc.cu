@@ -180,20 +180,6 @@ __device__ __forceinline__ void split2(float v, unsigned short& hi, unsigned sho
   }
 }
 
-template <bool BF16>
-__device__ __forceinline__ void store8(unsigned char* hi_base, unsigned char* lo_base,
-                                       unsigned off, const float (&v)[8]) {
-  unsigned short h[8], l[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) split2<BF16>(v[e], h[e], l[e]);
-  *reinterpret_cast<uint4*>(hi_base + off) =
-      make_uint4(h[0] | ((unsigned)h[1] << 16), h[2] | ((unsigned)h[3] << 16),
-                 h[4] | ((unsigned)h[5] << 16), h[6] | ((unsigned)h[7] << 16));
-  *reinterpret_cast<uint4*>(lo_base + off) =
-      make_uint4(l[0] | ((unsigned)l[1] << 16), l[2] | ((unsigned)l[3] << 16),
-                 l[4] | ((unsigned)l[5] << 16), l[6] | ((unsigned)l[7] << 16));
-}
-
 // Spectrum of one channel for the tensor-core producers (GAUSSIAN: the
 // erf difference across the channel, with erfc in the tails so that the
 // far wings of many lines do not accumulate cancellation error; DIRAC; TABLE).
@@ -279,12 +265,22 @@ __device__ __forceinline__ float kt_eval_smem(const KTableInfo& inf, const float
 
 // 16-bit hi/lo halves of two values packed as (first | second << 16).
 template <bool BF16>
+// Packed conversions round each element as the scalar ones do (same bits
+// as split2 per value), with one conversion per pair.
 __device__ __forceinline__ void split_pair(float a, float b, unsigned& hi, unsigned& lo) {
-  unsigned short ah, al, bh, bl;
-  split2<BF16>(a, ah, al);
-  split2<BF16>(b, bh, bl);
-  hi = (unsigned)ah | ((unsigned)bh << 16);
-  lo = (unsigned)al | ((unsigned)bl << 16);
+  if (BF16) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const unsigned*>(&h);
+    lo = *reinterpret_cast<const unsigned*>(&l);
+  } else {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const unsigned*>(&h);
+    lo = *reinterpret_cast<const unsigned*>(&l);
+  }
 }
 
 // W of one particle at the four pixels of a lane: rows ib + 2 k, column j.
