@@ -124,6 +124,17 @@ class InsertionEngine:
         N.check(self.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
                                    self._caps[0], self._caps[1], C.c_void_p(s.cuda_stream)))
 
+    def capture(self, prob: N.Problem) -> "torch.cuda.CUDAGraph":
+        """Capture mg_insert of ``prob`` (after :meth:`plan`) in a CUDA graph:
+        ``graph.replay()`` then runs the whole insertion as one launch.  The
+        problem's buffers and this engine's workspace must stay in place."""
+        self.run(prob)  # first call sets the kernels' attributes outside the capture
+        torch.cuda.synchronize(self.device)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            self.run(prob)
+        return graph
+
     def run_stages(self, prob: N.Problem, stages: int, stream=None) -> None:
         """Some stages of mg_insert (N.MG_STAGE_* bits), asynchronous."""
         s = stream or torch.cuda.current_stream(self.device)
