@@ -55,7 +55,7 @@ int channel_bits(int nc) {
 
 struct Layout {
   size_t hdr, gal, gst, gp0, gt0, gs0, ge0, gr0, rec, npairs, pair_off, tile_count, tile_diff,
-      tile_wlo, tile_whi, tile_off, ehi, elo, inv_w, keys, list, keys_tmp, list_tmp, rs_hist,
+      tile_off, ehi, elo, inv_w, keys, list, keys_tmp, list_tmp, rs_hist,
       rs_off, scan_sums, seg_lo, seg_hi, seg_items, seg_part, item_off, part_off, partial,
       flux_part, total;
 };
@@ -89,8 +89,6 @@ Layout layout(const Geo& g, long long cap_pairs, long long cap_partial) {
   L.pair_off = take(sizeof(long long) * nn);
   L.tile_count = take(sizeof(int) * (size_t)g.ntiles);
   L.tile_diff = take(sizeof(int) * (size_t)g.ndiff);
-  L.tile_wlo = take(sizeof(int) * (size_t)g.ntiles);
-  L.tile_whi = take(sizeof(int) * (size_t)g.ntiles);
   L.tile_off = take(sizeof(long long) * ((size_t)g.ntiles + 1));
   L.ehi = take(sizeof(float) * (size_t)g.nedge);
   L.elo = take(sizeof(float) * (size_t)g.nedge);
@@ -131,8 +129,6 @@ Ws make_ws(void* base, const Layout& L) {
   w.pair_off = reinterpret_cast<long long*>(b + L.pair_off);
   w.tile_count = reinterpret_cast<int*>(b + L.tile_count);
   w.tile_diff = reinterpret_cast<int*>(b + L.tile_diff);
-  w.tile_wlo = reinterpret_cast<int*>(b + L.tile_wlo);
-  w.tile_whi = reinterpret_cast<int*>(b + L.tile_whi);
   w.tile_off = reinterpret_cast<long long*>(b + L.tile_off);
   w.ehi = reinterpret_cast<float*>(b + L.ehi);
   w.elo = reinterpret_cast<float*>(b + L.elo);
@@ -317,15 +313,18 @@ int make_batch(const mg_problem* probs, int nprob, Batch* b, bool shape_only = f
   return MG_OK;
 }
 
+// SM count of the current device (cached per device).
 int num_sms() {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
+  constexpr int kMaxDev = 64;
+  static int sms[kMaxDev] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 1;
+  if (sms[dev] <= 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = v > 0 ? v : 1;
   }
-  return sms;
+  return sms[dev];
 }
 
 bool tc_form(int form) { return form == MG_FORM_BF16X3 || form == MG_FORM_F16X3; }

@@ -170,20 +170,15 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
       if (ok) {
         const int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
         const int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
-        np = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+        // one pair per (tile, channel block) the line meets
+        const int nb = G.ncb > 1 ? rec.chi / G.width - rec.clo / G.width + 1 : 1;
+        np = (tx1 - tx0 + 1) * (ty1 - ty0 + 1) * nb;
         const int dw = G.nty + 1;
         int* const diff = smem_hist ? s_diff : w.tile_diff + G.diff0;
         atomicAdd(&diff[tx0 * dw + ty0], 1);
         atomicAdd(&diff[tx0 * dw + ty1 + 1], -1);
         atomicAdd(&diff[(tx1 + 1) * dw + ty0], -1);
         atomicAdd(&diff[(tx1 + 1) * dw + ty1 + 1], 1);
-        if (G.ncb > 1)
-          for (int tx = tx0; tx <= tx1; ++tx)
-            for (int ty = ty0; ty <= ty1; ++ty) {
-              const int t = G.tile0 + tx * G.nty + ty;
-              atomicMin(&w.tile_wlo[t], rec.clo);
-              atomicMax(&w.tile_whi[t], rec.chi);
-            }
         wmax_v = rec.chi - rec.clo;
         my_spec += (unsigned)(rec.chi - rec.clo + 1);
         if (g.form == MG_FORM_F16X3) {
@@ -232,10 +227,6 @@ __global__ void k_tile_init(Geo g, Ws w, long long cap_pairs, long long cap_part
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.ndiff; t += stride)
     w.tile_diff[t] = 0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.ntiles; t += stride) {
-    w.tile_wlo[t] = 0x7fffffff;
-    w.tile_whi[t] = -1;
-  }
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < g.ngal; k += stride) {
     GalState z;
     z.dec = 0;
@@ -323,12 +314,13 @@ __global__ void k_diff_prefix(Geo g, Ws w, int smem_cap) {
   }
 }
 
-// After the scan of the tile counts (total in tile_off[ntiles]): the work
-// item size from the total, the split-K bound with it (every segment of a
-// tile holds at most the tile's count) and the pair-capacity check.
+// After the scans of the pair counts (total in hdr->n_pairs) and the tile
+// counts: the work item size from the total pairs, the split-K bound with it
+// (every segment of a tile lists at most the tile's particles, each once)
+// and the pair-capacity check.
 __global__ void k_plan_finish(Geo g, Ws w, int num_sms) {
   __shared__ long long red[256];
-  const long long total = w.tile_off[g.ntiles];
+  const long long total = w.hdr->n_pairs;
   const int kch = item_particles(total, num_sms);
   long long sb = 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.ntiles; t += gridDim.x * blockDim.x) {
@@ -347,13 +339,13 @@ __global__ void k_plan_finish(Geo g, Ws w, int num_sms) {
               (unsigned long long)red[0]);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     WsHeader* h = w.hdr;
-    h->n_pairs = total;
     h->kch = kch;
     if (total > h->cap_pairs) atomicOr(&h->status, ST_PAIRS);
   }
 }
 
-// Pairs in particle order: key = global tile << cbits | clo, value = particle.
+// Pairs in particle order: key = global segment << cbits | clo (one pair per
+// tile and channel block the particle's line meets), value = particle.
 __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict__ vals) {
   if (w.hdr->status & (ST_PAIRS | ST_EDGES)) return;
   for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < g.n;
@@ -364,13 +356,16 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
     long long o = w.pair_off[P];
     const int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
     const int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
+    const int cb0 = G.ncb > 1 ? rec.clo / G.width : 0;
+    const int cb1 = G.ncb > 1 ? rec.chi / G.width : 0;
     for (int tx = tx0; tx <= tx1; ++tx)
-      for (int ty = ty0; ty <= ty1; ++ty) {
-        const unsigned t = (unsigned)(G.tile0 + tx * G.nty + ty);
-        keys[o] = (t << g.cbits) | (unsigned)rec.clo;
-        vals[o] = (int)P;
-        ++o;
-      }
+      for (int ty = ty0; ty <= ty1; ++ty)
+        for (int cb = cb0; cb <= cb1; ++cb) {
+          const unsigned sg = (unsigned)(G.seg0 + (tx * G.nty + ty) * G.ncb + cb);
+          keys[o] = (sg << g.cbits) | (unsigned)rec.clo;
+          vals[o] = (int)P;
+          ++o;
+        }
   }
 }
 
@@ -384,38 +379,21 @@ __device__ __forceinline__ long long lower_bound_keys(const unsigned* keys, long
   return lo;
 }
 
-// One thread per segment (tile, channel block): the sorted-list range of the
-// particles whose support [clo, chi] can meet the block (clo within
-// [c0 - wmax, c0 + width)), its K chunks and its split-K partial items.
+// One thread per segment (tile, channel block): its range of the sorted
+// list (keys segment << cbits | clo, so the segment's particles are exactly
+// the keys in [segment << cbits, (segment + 1) << cbits)), its K chunks and
+// its split-K partial items.
 __global__ void k_segments(Geo g, Ws w) {
   const bool bad = (w.hdr->status & (ST_PAIRS | ST_EDGES)) != 0;
   const int kch = w.hdr->kch;
-  const unsigned cmask_hi = (1u << g.cbits);
+  const long long n = w.hdr->n_pairs;
   for (int sg = blockIdx.x * blockDim.x + threadIdx.x; sg < g.nseg; sg += gridDim.x * blockDim.x) {
-    const int gk = find_gal(w.gs0, g.ngal, sg);
-    const Gal& G = w.gal[gk];
-    const int ls = sg - G.seg0;
-    const int t = G.tile0 + ls / G.ncb;
-    const int cb = ls - (ls / G.ncb) * G.ncb;
-    long long lo = w.tile_off[t], hi = w.tile_off[t + 1];
+    long long lo = 0, hi = 0;
     int items = 0, part = 0;
-    if (!bad && hi > lo) {
-      if (G.ncb > 1) {
-        const int wmax = w.gst[gk].wmax;
-        const int c0 = cb * G.width;
-        const int clo_min = c0 - wmax > 0 ? c0 - wmax : 0;
-        const unsigned c_end = (unsigned)(c0 + G.width);  // first clo past the block
-        const unsigned tk = (unsigned)t << g.cbits;
-        const long long a = lower_bound_keys(w.keys, lo, hi, tk | (unsigned)clo_min);
-        const long long b = c_end >= cmask_hi ? hi : lower_bound_keys(w.keys, a, hi, tk | c_end);
-        // skip blocks entirely outside the tile's channel window
-        if (c0 > w.tile_whi[t] || c0 + G.width <= w.tile_wlo[t]) {
-          lo = hi = a;
-        } else {
-          lo = a;
-          hi = b;
-        }
-      }
+    if (!bad && n > 0) {
+      lo = lower_bound_keys(w.keys, 0, n, (unsigned)sg << g.cbits);
+      hi = sg + 1 == g.nseg ? n
+                            : lower_bound_keys(w.keys, lo, n, (unsigned)(sg + 1) << g.cbits);
       const long long cnt = hi - lo;
       if (cnt > 0) {
         items = (int)((cnt + kch - 1) / kch);
@@ -457,7 +435,7 @@ void launch_prep(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, long lo
     if (smem_hist && blocks > per_sm * (unsigned)num_sms) blocks = per_sm * (unsigned)num_sms;
     k_prep<<<blocks, PREP_THREADS, hist_bytes, s>>>(g, w);
   }
-  launch_scan(w.npairs, g.n, w.pair_off, w.scan_sums, nullptr, s);
+  launch_scan(w.npairs, g.n, w.pair_off, w.scan_sums, &w.hdr->n_pairs, s);
   // per-cube prefix sums of the difference arrays, in up to 200 KB of
   // dynamic shared memory (the attribute is per device: set on every launch)
   constexpr int kPlanSmemCap = 50 * 1024;
@@ -474,9 +452,9 @@ void launch_prep(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, long lo
 }
 
 int sort_bits(const Geo& g) {
-  int tbits = 0;
-  while ((1LL << tbits) < (long long)g.ntiles) ++tbits;
-  return tbits + g.cbits;
+  int sbits = 0;
+  while ((1LL << sbits) < (long long)g.nseg) ++sbits;
+  return sbits + g.cbits;
 }
 
 // Tile-major list sorted by (tile, clo), then the segments with their

@@ -177,13 +177,11 @@ struct Ws {
   long long* pair_off;   // [n] exclusive scan of npairs
   int* tile_count;       // [ntiles]
   int* tile_diff;        // [ndiff] per cube (ntx + 1) x (nty + 1) difference arrays
-  int* tile_wlo;         // [ntiles]
-  int* tile_whi;         // [ntiles]
   long long* tile_off;   // [ntiles + 1] pair offsets (tile-major sorted list)
   float* ehi;            // [nedge] edges, double-float high part
   float* elo;            // [nedge] low part
   float* inv_w;          // [nedge] 1 / |channel width| (channel c of a cube at edge0 + c)
-  unsigned* keys;        // [cap_pairs] sorted keys: tile << cbits | clo
+  unsigned* keys;        // [cap_pairs] sorted keys: segment << cbits | clo
   int* list;             // [cap_pairs] particle ids in sorted order
   unsigned* keys_tmp;    // [cap_pairs] radix-sort second buffer
   int* list_tmp;         // [cap_pairs]

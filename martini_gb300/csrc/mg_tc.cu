@@ -918,16 +918,22 @@ int launch_tc(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, int nwmax)
   size_t smem = 2 * (2 * (size_t)KSTEPS * 4096 + 2 * (size_t)KSTEPS * nwmax * 32);
   // at least 116 KB so that one CTA (and its 512 TMEM columns) fits per SM
   if (smem < 118784) smem = 118784;
-  static int attr_bytes = -1;
-  if (attr_bytes < 0) {
+  // the shared-memory attribute is per device: set once on each (host-side
+  // calls, made before a graph capture by the first insertion on a device)
+  constexpr int kMaxDev = 64;
+  static int attr_bytes[kMaxDev] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return MG_ERR_CUDA;
+  if (attr_bytes[dev] <= 0) {
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, k_contract_tc<BF16, KC>) != cudaSuccess) return MG_ERR_CUDA;
-    attr_bytes = 227 * 1024 - (int)fa.sharedSizeBytes;
+    const int bytes = 227 * 1024 - (int)fa.sharedSizeBytes;
     if (cudaFuncSetAttribute(k_contract_tc<BF16, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             attr_bytes) != cudaSuccess)
+                             bytes) != cudaSuccess)
       return MG_ERR_CUDA;
+    attr_bytes[dev] = bytes;
   }
-  if ((int)smem > attr_bytes) return MG_ERR_UNSUPPORTED;
+  if ((int)smem > attr_bytes[dev]) return MG_ERR_UNSUPPORTED;
   k_contract_tc<BF16, KC><<<num_sms, TC_THREADS, smem, s>>>(g, w, nwmax);
   return MG_OK;
 }
