@@ -283,6 +283,21 @@ __device__ __forceinline__ void split_pair(float a, float b, unsigned& hi, unsig
   }
 }
 
+// GaussianKernel pixel integral (sph_kernels.py:994-1044), w_gaussian with
+// the per-particle quotients taken as products with reciprocals: the same
+// formula to an ulp or two, without six divisions per pixel.
+__device__ __forceinline__ float w_gaussian_tc(float dx, float dy, float inv_hs, float trunc,
+                                               float inv_gnorm) {
+  const float dr = sqrtf(dx * dx + dy * dy);
+  const float q = dr * inv_hs;
+  if ((dr - 0.70710678118654752f) * inv_hs > trunc) return 0.f;
+  const float zmax = trunc > q ? sqrtf(trunc * trunc - q * q) : 0.f;
+  const float s = inv_hs * 0.70710678118654752f;  // 1 / (h sqrt(2) sigma)
+  const float ex = erff((dx + 0.5f) * s) - erff((dx - 0.5f) * s);
+  const float ey = erff((dy + 0.5f) * s) - erff((dy - 0.5f) * s);
+  return 0.25f * erff(zmax * 0.70710678118654752f) * ex * ey * inv_gnorm;
+}
+
 // W of one particle at the four pixels of a lane: rows ib + 2 k, column j.
 __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec* ks,
                                          const float4* ktab, int ktab_type, int ib, int j,
@@ -304,9 +319,11 @@ __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec*
 #pragma unroll
     for (int k = 0; k < 4; ++k) w[k] = in[k] ? sw : 0.f;
   } else if (kk.type == MG_KERNEL_GAUSSIAN) {
+    const float inv_hs = 1.f / (r.h * 0.42466090014400953f);  // 1 / (h sigma_FWHM)
+    const float inv_gnorm = 1.f / kk.gnorm;
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      w[k] = in[k] ? w_gaussian(dx[k], dy, r.h, kk.truncate, kk.gnorm) * sw : 0.f;
+      w[k] = in[k] ? w_gaussian_tc(dx[k], dy, inv_hs, kk.truncate, inv_gnorm) * sw : 0.f;
   } else {
     const KTableInfo& inf = kt_info[kk.type];
     const float fac = (kk.type == MG_KERNEL_CUBIC_SPLINE ? 4.f : 1.f) * r.inv_h2;
@@ -547,7 +564,6 @@ template <bool BF16, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
   constexpr int KSTEPS = KC / 16;
-  constexpr int GROUPS = KC / 8;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
