@@ -345,27 +345,63 @@ __global__ void k_plan_finish(Geo g, Ws w, int num_sms) {
 }
 
 // Pairs in particle order: key = global segment << cbits | clo (one pair per
-// tile and channel block the particle's line meets), value = particle.
+// tile and channel block the particle's line meets), value = particle.  A
+// warp takes 32 particles and writes them one at a time with all its lanes,
+// so the stores of a particle's pairs are contiguous; each pair's position
+// pair_off[P] + e is the same as in a particle-per-thread loop.
 __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict__ vals) {
   if (w.hdr->status & (ST_PAIRS | ST_EDGES)) return;
-  for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < g.n;
-       P += (long long)gridDim.x * blockDim.x) {
-    const PRec rec = w.rec[P];
-    if (rec.ilo > rec.ihi) continue;
-    const Gal& G = w.gal[find_gal(w.gp0, g.ngal, P)];
-    long long o = w.pair_off[P];
-    const int tx0 = rec.ilo / TILE_I, tx1 = rec.ihi / TILE_I;
-    const int ty0 = rec.jlo / TILE_J, ty1 = rec.jhi / TILE_J;
-    const int cb0 = G.ncb > 1 ? rec.clo / G.width : 0;
-    const int cb1 = G.ncb > 1 ? rec.chi / G.width : 0;
-    for (int tx = tx0; tx <= tx1; ++tx)
-      for (int ty = ty0; ty <= ty1; ++ty)
-        for (int cb = cb0; cb <= cb1; ++cb) {
-          const unsigned sg = (unsigned)(G.seg0 + (tx * G.nty + ty) * G.ncb + cb);
-          keys[o] = (sg << g.cbits) | (unsigned)rec.clo;
-          vals[o] = (int)P;
-          ++o;
-        }
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32;
+       base < g.n; base += nwarps * 32) {
+    const long long P = base + lane;
+    // this lane's particle: first pair, pair count and the parameters of its
+    // tile / block ranges
+    long long o = 0;
+    int np = 0, tx0 = 0, ty0 = 0, nty_span = 1, cb0 = 0, nb = 1, clo = 0, seg0 = 0, nty = 1,
+        ncb = 1;
+    if (P < g.n) {
+      const PRec rec = w.rec[P];
+      if (rec.ilo <= rec.ihi) {
+        const Gal& G = w.gal[find_gal(w.gp0, g.ngal, P)];
+        o = w.pair_off[P];
+        np = w.npairs[P];
+        tx0 = rec.ilo / TILE_I;
+        ty0 = rec.jlo / TILE_J;
+        nty_span = rec.jhi / TILE_J - ty0 + 1;
+        cb0 = G.ncb > 1 ? rec.clo / G.width : 0;
+        nb = G.ncb > 1 ? rec.chi / G.width - cb0 + 1 : 1;
+        clo = rec.clo;
+        seg0 = G.seg0;
+        nty = G.nty;
+        ncb = G.ncb;
+      }
+    }
+    for (int src = 0; src < 32; ++src) {
+      const int cnt = __shfl_sync(0xffffffffu, np, src);
+      if (cnt == 0) continue;  // warp-uniform
+      const long long so = __shfl_sync(0xffffffffu, o, src);
+      const int stx0 = __shfl_sync(0xffffffffu, tx0, src);
+      const int sty0 = __shfl_sync(0xffffffffu, ty0, src);
+      const int sspan = __shfl_sync(0xffffffffu, nty_span, src);
+      const int scb0 = __shfl_sync(0xffffffffu, cb0, src);
+      const int snb = __shfl_sync(0xffffffffu, nb, src);
+      const int sclo = __shfl_sync(0xffffffffu, clo, src);
+      const int sseg0 = __shfl_sync(0xffffffffu, seg0, src);
+      const int snty = __shfl_sync(0xffffffffu, nty, src);
+      const int sncb = __shfl_sync(0xffffffffu, ncb, src);
+      const int sp = (int)(base + src);
+      for (int e = lane; e < cnt; e += 32) {
+        // pair e: tiles row-major over (tx, ty), then the channel blocks
+        const int cb = scb0 + e % snb;
+        const int t = e / snb;
+        const int tx = stx0 + t / sspan, ty = sty0 + t % sspan;
+        const unsigned sg = (unsigned)(sseg0 + (tx * snty + ty) * sncb + cb);
+        keys[so + e] = (sg << g.cbits) | (unsigned)sclo;
+        vals[so + e] = sp;
+      }
+    }
   }
 }
 

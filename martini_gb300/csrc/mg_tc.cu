@@ -962,7 +962,9 @@ void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
   const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, (long long)num_sms * 16);
   k_spec_count<<<blocks, 256, 0, s>>>(g, w);
   launch_scan(w.npairs, n, w.pair_off, w.scan_sums, &w.hdr->n_spec, s);
-  const unsigned eblocks = (unsigned)std::min<long long>((n + 7) / 8, (long long)num_sms * 16);
+  // a warp per particle, many warps in flight (each particle's work is a
+  // short dependent chain: record, offsets, erfc)
+  const unsigned eblocks = (unsigned)std::min<long long>((n + 7) / 8, (long long)num_sms * 64);
   k_spec_eval<<<eblocks, 256, 0, s>>>(g, w);
 }
 
