@@ -14,7 +14,11 @@ term).  Cells are aligned with every shell radius, so each cell's function
 is smooth; the log term at R = 0 (f ~ R^4 log R) is far below FP32 resolution
 on the first cell.  The FP32 device evaluation is emulated here and its
 error against the FP64 formula is written into the header.  The device
-computes the cell index directly (no search) and runs one Horner sweep.
+computes the cell index directly (no search), loads the cell's four
+coefficients as one float4 and runs a three-FMA Horner sweep.  Cubic pieces
+reach the FP32 floor (~1e-7 of f(0)) on 256-576 cells; the Wendland C6
+profile, whose closed form itself carries rounded constants, takes 2048
+cells to stay within its FP64 formula's own ~7e-7.
 
 Run:  python martini_gb300/csrc/gen_kernel_tables.py   (writes the header
 next to this file; the header is committed).
@@ -26,7 +30,7 @@ import os
 
 import numpy as np
 
-DEG = 7  # polynomial degree per cell (8 coefficients = two float4 loads)
+DEG = 3  # polynomial degree per cell (4 coefficients = one float4 load)
 
 # ---- FP64 profiles (value of the pixel integral times h^2 / norm) -----------
 
@@ -121,7 +125,7 @@ KERNELS = [
     ("WENDLAND_C2", 0, f_wendland_c2, 1.0, "21.0 / (2.0 * 3.14159265358979323846)",
      [("R", 0.0, 1.0, 256)]),
     ("WENDLAND_C6", 1, f_wendland_c6, 1.0, "1365.0 / (64.0 * 3.14159265358979323846)",
-     [("R", 0.0, 1.0, 512)]),
+     [("R", 0.0, 1.0, 2048)]),
     ("CUBIC_SPLINE", 2, f_cubic_spline, 4.0, "4.0 / 1.59689476201133",
      [("R", 0.0, 0.75, 192), ("A", 0.0, float(np.sqrt(1 - 0.75**2)), 128), ("R", 1.0, 2.0, 256)]),
     ("QUARTIC_SPLINE", 3, f_quartic_spline, 1.0, "2.0 * 15625.0 / (512.0 * 3.14159265358979323846)",
@@ -242,7 +246,7 @@ def main():
     body.append("")
     flat = np.concatenate(all_coefs).ravel()
     body.append(f"// {ncoef_cells} cells x {DEG + 1} coefficients (t^0 .. t^{DEG}), t in [0, 1)")
-    body.append(f"__device__ const float kt_coef[{len(flat)}] = {{")
+    body.append(f"__device__ __align__(16) const float kt_coef[{len(flat)}] = {{")
     for i in range(0, len(flat), DEG + 1):
         body.append("    " + ", ".join(f"{float(v):.9g}f" for v in flat[i:i + DEG + 1]) + ",")
     body.append("};")

@@ -299,10 +299,11 @@ constexpr float kPi = 3.14159265358979323846f;
 // Radial kernels (WendlandC2 sph_kernels.py:400-441, WendlandC6 :544-685,
 // cubic spline :791-858, quartic spline :1486-1564): the pixel integral is
 // scale * f(s) / h^2 with s = R^2 (offsets doubled for the cubic spline).
-// f comes from degree-7 polynomials on uniform cells fitted in FP64 to the
+// f comes from cubic polynomials on uniform cells fitted in FP64 to the
 // reference closed forms (mg_kernel_tables.h, made by gen_kernel_tables.py):
-// a direct cell index and one Horner sweep, accurate to ~1e-7 of f(0) in
-// FP32 where the closed forms lose up to 7e-4.
+// a direct cell index, one float4 of coefficients and three FMAs, accurate
+// to ~1e-7 of f(0) in FP32 (7e-7 for Wendland C6) where the closed forms
+// lose up to 7e-4.
 __device__ __forceinline__ float kt_eval(int kt, float s) {
   const KTableInfo& inf = kt_info[kt];
   if (!(s < inf.smax)) return 0.f;
@@ -316,16 +317,9 @@ __device__ __forceinline__ float kt_eval(int kt, float s) {
   int c = (int)u;
   c = c < 0 ? 0 : (c >= g.ncell ? g.ncell - 1 : c);
   const float t = u - (float)c;
-  const float4* c4 = reinterpret_cast<const float4*>(kt_coef) + 2 * (g.first + c);
-  const float4 lo = __ldg(c4), hi = __ldg(c4 + 1);
-  float acc = hi.w;
-  acc = fmaf(acc, t, hi.z);
-  acc = fmaf(acc, t, hi.y);
-  acc = fmaf(acc, t, hi.x);
-  acc = fmaf(acc, t, lo.w);
-  acc = fmaf(acc, t, lo.z);
-  acc = fmaf(acc, t, lo.y);
-  return fmaf(acc, t, lo.x);
+  static_assert(KT_DEG == 3, "one float4 of coefficients per cell");
+  const float4 cf = __ldg(reinterpret_cast<const float4*>(kt_coef) + g.first + c);
+  return fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
 }
 
 __device__ __forceinline__ float w_radial(int kt, float r2, float inv_h2) {

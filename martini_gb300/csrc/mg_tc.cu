@@ -39,8 +39,17 @@ constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
 // round-to-nearest FP32 adds, which bounds that drift to ~TC_DRAIN * 3 * KC/16
 // MMAs per partial sum.
 constexpr int TC_DRAIN = 2;
-constexpr int KT_SMEM_CELLS = 576;  // largest radial table (cubic spline)
+// Radial tables up to this many cells (one float4 each: the cubic spline's
+// 576, WendlandC2, quartic spline) are copied to shared memory; WendlandC6's
+// 2048 are read through L1.
+constexpr int KT_SMEM_CELLS = 576;
 constexpr int TC_MASTER_COL = 256;
+// Shared memory at the widest band: two stages of A and B hi/lo tiles
+// (KC = 64) plus the static arrays must fit in the 227 KB of a CTA.
+static_assert(2 * (2 * 4 * 4096 + 2 * 4 * TC_MASTER_COL * 32) + KT_SMEM_CELLS * 16 +
+                      2 * 64 * (sizeof(PRec) + sizeof(int) + sizeof(long long)) + 4096 <=
+                  227 * 1024,
+              "tensor-core kernel shared memory");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -252,14 +261,9 @@ __device__ __forceinline__ float kt_eval_smem(const KTableInfo& inf, const float
   const float u = (v - g.lo) * g.cells_per_unit;
   const int c = min(max(__float2int_rz(u), 0), g.ncell - 1);
   const float t = u - (float)c;
-  const float4 lo = tab[2 * (g.first + c)];
-  const float4 hi = tab[2 * (g.first + c) + 1];
-  // Estrin: (c0 + c1 t) + t^2 (c2 + c3 t) + t^4 ((c4 + c5 t) + t^2 (c6 + c7 t))
-  const float t2 = t * t;
-  const float t4 = t2 * t2;
-  const float p01 = fmaf(lo.y, t, lo.x), p23 = fmaf(lo.w, t, lo.z);
-  const float p45 = fmaf(hi.y, t, hi.x), p67 = fmaf(hi.w, t, hi.z);
-  const float f = fmaf(t4, fmaf(t2, p67, p45), fmaf(t2, p23, p01));
+  static_assert(KT_DEG == 3, "one float4 of coefficients per cell");
+  const float4 cf = tab[g.first + c];
+  const float f = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
   return s < inf.smax ? f : 0.f;
 }
 
@@ -569,7 +573,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   __shared__ int s_pid[2][KC];
   __shared__ long long s_soff[2][KC];  // spectrum store rows
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
-  __shared__ float4 s_ktab[2 * KT_SMEM_CELLS];
+  __shared__ float4 s_ktab[KT_SMEM_CELLS];
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
@@ -601,8 +605,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     int ncell = 0;
     for (int r = 0; r < inf.nreg; ++r) ncell += inf.reg[r].ncell;
     if (ncell <= KT_SMEM_CELLS) {
-      const float4* src = reinterpret_cast<const float4*>(kt_coef) + 2 * inf.reg[0].first;
-      for (int e = tid; e < 2 * ncell; e += TC_THREADS) s_ktab[e] = src[e];
+      const float4* src = reinterpret_cast<const float4*>(kt_coef) + inf.reg[0].first;
+      for (int e = tid; e < ncell; e += TC_THREADS) s_ktab[e] = src[e];
     } else {
       ktab_type = -1;
     }
@@ -783,7 +787,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
           pf2 = spec_at(spec, so0, r0, v0, wa + 32 + lane);
           pf3 = spec_at(spec, so1, r1, v1, wa + 32 + lane);
         }
-        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - 2 * (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
+        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
                              ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
         produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
                              w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
