@@ -8,17 +8,16 @@ directly in FP32 they lose up to 2e-6 (C2), 3e-6 (cubic), 6e-6 (quartic) and
 7e-4 (C6) of the peak value.  Here each profile f(s), s = R^2 (R = distance /
 rescaled smoothing length; offsets doubled for the cubic spline, as the
 reference does), is evaluated in FP64 from the reference formula and fitted
-by Chebyshev interpolation on uniform cells in R (and, just inside the
-cubic spline's inner shell, in A = sqrt(1 - R^2), where f has a (1 - R)^1.5
-term).  Cells are aligned with every shell radius, so each cell's function
-is smooth; the log term at R = 0 (f ~ R^4 log R) is far below FP32 resolution
-on the first cell.  The FP32 device evaluation is emulated here and its
-error against the FP64 formula is written into the header.  The device
-computes the cell index directly (no search), loads the cell's four
-coefficients as one float4 and runs a three-FMA Horner sweep.  Cubic pieces
-reach the FP32 floor (~1e-7 of f(0)) on 256-576 cells; the Wendland C6
-profile, whose closed form itself carries rounded constants, takes 2048
-cells to stay within its FP64 formula's own ~7e-7.
+by Chebyshev interpolation with cubic polynomials on uniform cells: in s for
+the Wendland and quartic kernels, in R (and, just inside the cubic spline's
+inner shell, in A = sqrt(1 - R^2), where f has a (1 - R)^1.5 term) for the
+cubic spline, whose cells are aligned with its shell radius.  The FP32
+device evaluation is emulated here and its error against the FP64 formula is
+written into the header.  The device computes the cell index directly (no
+search), loads the cell's four coefficients as one float4 and runs a
+three-FMA Horner sweep.  The pieces reach the FP32 floor (~1e-7 of f(0)); the
+Wendland C6 closed form itself carries rounded constants, and its table
+stays within that formula's own ~7e-7.
 
 Run:  python martini_gb300/csrc/gen_kernel_tables.py   (writes the header
 next to this file; the header is committed).
@@ -115,25 +114,33 @@ def f_quartic_spline(s):
 
 
 # Regions of each profile, each a uniform grid of cells in one variable:
+#   ("S", 0, s_max, ncell) v = s = R^2, followed by one all-zero cell: the
+#                          device clamps the cell coordinate u = s * ncell /
+#                          s_max to ncell, so every s >= s_max lands on the
+#                          zero cell and needs no support test
 #   ("R", lo, hi, ncell)   v = R
 #   ("A", lo, hi, ncell)   v = sqrt(1 - R^2), used just inside a shell at R = 1
-# Cells are aligned with the shell radii (quartic: 0.2, 0.6; cubic: 1 in
-# doubled offsets), so each cell's function is smooth; the half-integer power
-# of the cubic spline's inner shell, (1 - R)^1.5, is resolved by the A grid.
+# The Wendland and quartic profiles are smooth enough in s (the s^2 log s
+# term of WendlandC2 at s = 0 sets its cell count), so the device needs no
+# square root.  The cubic spline keeps cells in R aligned with its shell at
+# R = 1 (doubled offsets), with the half-integer power of the inner shell,
+# (1 - R)^1.5, resolved by the A grid.
 KERNELS = [
     # name, code, profile, support s_max = R_max^2, device scale, regions
     ("WENDLAND_C2", 0, f_wendland_c2, 1.0, "21.0 / (2.0 * 3.14159265358979323846)",
-     [("R", 0.0, 1.0, 256)]),
+     [("S", 0.0, 1.0, 1024)]),
     ("WENDLAND_C6", 1, f_wendland_c6, 1.0, "1365.0 / (64.0 * 3.14159265358979323846)",
-     [("R", 0.0, 1.0, 2048)]),
+     [("S", 0.0, 1.0, 1024)]),
     ("CUBIC_SPLINE", 2, f_cubic_spline, 4.0, "4.0 / 1.59689476201133",
      [("R", 0.0, 0.75, 192), ("A", 0.0, float(np.sqrt(1 - 0.75**2)), 128), ("R", 1.0, 2.0, 256)]),
     ("QUARTIC_SPLINE", 3, f_quartic_spline, 1.0, "2.0 * 15625.0 / (512.0 * 3.14159265358979323846)",
-     [("R", 0.0, 1.0, 320)]),
+     [("S", 0.0, 1.0, 512)]),
 ]
 
 
 def region_fn(f, var):
+    if var == "S":
+        return f
     if var == "R":
         return lambda v: f(v**2)
     return lambda v: f(1 - v**2)
@@ -154,16 +161,32 @@ def fit_cells(fv, lo, hi, ncell):
     return np.array(out, dtype=np.float32)
 
 
+def region_cells(regions):
+    """Table entries (float4 cells) of each region: S regions carry one zero
+    cell after their ncell fitted ones."""
+    return [n + (1 if var == "S" else 0) for var, lo, hi, n in regions]
+
+
 def device_eval(regions, coefs, smax, s):
     """FP32 emulation of kt_eval in mg_internal.cuh."""
     s32 = s.astype(np.float32)
+    if regions[0][0] == "S":
+        var, lo, hi, ncell = regions[0]
+        u = np.minimum(s32 * np.float32(ncell / (hi - lo)), np.float32(ncell)).astype(np.float32)
+        c = np.floor(u).astype(np.int64)
+        t = (u - c.astype(np.float32)).astype(np.float32)
+        cf = coefs[c]
+        acc = cf[:, -1].copy()
+        for k in range(DEG - 1, -1, -1):
+            acc = (acc * t + cf[:, k]).astype(np.float32)
+        return acc.astype(np.float64)
     R = np.sqrt(s32)
     out = np.zeros(s.shape)
     reg_idx = np.zeros(s.shape, dtype=int)
     if len(regions) == 3:
         reg_idx[R >= np.float32(regions[0][2])] = 1
         reg_idx[s32 > np.float32(1.0)] = 2
-    first = np.cumsum([0] + [r[3] for r in regions])
+    first = np.cumsum([0] + region_cells(regions))
     for ri, (var, lo, hi, ncell) in enumerate(regions):
         m = (reg_idx == ri) & (s32 < np.float32(smax))
         if var == "R":
@@ -181,6 +204,14 @@ def device_eval(regions, coefs, smax, s):
     return out
 
 
+def c_float(v):
+    """A float literal of C: nine significant digits and a point or exponent."""
+    t = f"{float(v):.9g}"
+    if "." not in t and "e" not in t:
+        t += ".0"
+    return t + "f"
+
+
 def main():
     rng = np.random.default_rng(0)
     hdr = [
@@ -195,23 +226,28 @@ def main():
     ncoef_cells = 0
     for name, code, f, smax, scale, regions in KERNELS:
         f0 = float(f(np.array([0.0]))[0])
-        coefs = np.concatenate([fit_cells(region_fn(f, var), lo, hi, n)
-                                for var, lo, hi, n in regions])
+        parts = []
+        for var, lo, hi, n in regions:
+            parts.append(fit_cells(region_fn(f, var), lo, hi, n))
+            if var == "S":
+                parts.append(np.zeros((1, DEG + 1), dtype=np.float32))
+        coefs = np.concatenate(parts)
         s = np.concatenate((rng.uniform(0, smax, 400000), smax * 10 ** rng.uniform(-12, 0, 100000),
-                            np.clip(1 + rng.uniform(-1e-3, 1e-3, 50000), 0, smax)))
+                            np.clip(1 + rng.uniform(-1e-3, 1e-3, 50000), 0, smax),
+                            rng.uniform(smax, 4 * smax, 20000)))
         err = np.abs(device_eval(regions, coefs, smax, s)
-                     - f(s.astype(np.float32).astype(np.float64))).max() / f0
+                     - f(np.minimum(s.astype(np.float32).astype(np.float64), 2 * smax))).max() / f0
         hdr.append(f"//   {name}: {len(coefs)} cells, FP32 device-form max error {err:.2e} of f(0)")
         print(name, len(coefs), f"{err:.2e}")
         regs = []
         first = ncoef_cells
-        for var, lo, hi, n in regions:
-            regs.append((1 if var == "A" else 0, lo, n / (hi - lo), n, first))
-            first += n
+        for (var, lo, hi, n), cells in zip(regions, region_cells(regions)):
+            regs.append(({"R": 0, "A": 1, "S": 2}[var], lo, n / (hi - lo), n, first))
+            first += cells
         while len(regs) < 3:
             regs.append((0, 0.0, 0.0, 1, first - 1))
         split_r = regions[0][2] if len(regions) == 3 else 1e30
-        infos.append((smax, scale, len(regions), split_r, regs))
+        infos.append((smax, scale, len(regions), split_r, len(coefs), regs))
         all_coefs.append(coefs)
         ncoef_cells += len(coefs)
     body += [
@@ -222,7 +258,7 @@ def main():
         f"constexpr int KT_DEG = {DEG};",
         "",
         "struct KRegion {",
-        "  int var;         // 0: v = R, 1: v = sqrt(1 - R^2)",
+        "  int var;         // 0: v = R, 1: v = sqrt(1 - R^2), 2: v = s (zero cell after the last)",
         "  float lo;        // cell grid origin in v",
         "  float cells_per_unit;",
         "  int ncell;",
@@ -234,21 +270,22 @@ def main():
         "  float scale;     // norm multiplying f / h^2",
         "  int nreg;        // 1, or 3 for the cubic spline (R < split_r, s <= 1, s > 1)",
         "  float split_r;",
+        "  int ncoef;       // float4 cells of the table, zero cells included",
         "  KRegion reg[3];",
         "};",
         "",
         "__device__ __constant__ KTableInfo kt_info[4] = {",
     ]
-    for smax, scale, nreg, split_r, regs in infos:
+    for smax, scale, nreg, split_r, ncoef, regs in infos:
         rs = ", ".join(f"{{{v}, {lo!r}f, {cpu!r}f, {n}, {fi}}}" for v, lo, cpu, n, fi in regs)
-        body.append(f"    {{{smax!r}f, (float)({scale}), {nreg}, {split_r!r}f, {{{rs}}}}},")
+        body.append(f"    {{{smax!r}f, (float)({scale}), {nreg}, {split_r!r}f, {ncoef}, {{{rs}}}}},")
     body.append("};")
     body.append("")
     flat = np.concatenate(all_coefs).ravel()
     body.append(f"// {ncoef_cells} cells x {DEG + 1} coefficients (t^0 .. t^{DEG}), t in [0, 1)")
     body.append(f"__device__ __align__(16) const float kt_coef[{len(flat)}] = {{")
     for i in range(0, len(flat), DEG + 1):
-        body.append("    " + ", ".join(f"{float(v):.9g}f" for v in flat[i:i + DEG + 1]) + ",")
+        body.append("    " + ", ".join(c_float(v) for v in flat[i:i + DEG + 1]) + ",")
     body.append("};")
     body.append("")
     body.append("}  // namespace mg")

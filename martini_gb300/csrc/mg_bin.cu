@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
       rec.xi = rec.yi = 0;
       rec.xf = rec.yf = 0.f;
       rec.h = 1.f; rec.inv_h2 = 1.f;
-      rec.vhi = rec.vlo = 0.f; rec.inv_s = 0.f; rec.amp = 0.f; rec.pad_ = 0;
+      rec.vhi = rec.vlo = 0.f; rec.inv_s = 0.f; rec.amp = 0.f; rec.flags = 0;
       int ks = G.kidx ? (int)G.kidx[p] : 0;
       if (ks < 0 || ks >= g.n_kernels) ks = 0;  // -1: kernels[0] (sph_kernels.py:1360)
       rec.kslot = ks;
@@ -134,6 +134,13 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
         float h = G.h ? G.h[p] : 1.f;
         rec.h = h;
         rec.inv_h2 = 1.f / (h * h);
+        if (g.ks[ks].type <= MG_KERNEL_QUARTIC_SPLINE) {
+          // every table kernel reaches h px; rows outside the cube are never stored
+          const double reach = (double)h * (1.0 + 0x1p-20);
+          const bool lo_in = rec.ilo == 0 || x - (double)(rec.ilo - 1) >= reach;
+          const bool hi_in = rec.ihi == G.nx - 1 || (double)(rec.ihi + 1) - x >= reach;
+          if (lo_in && hi_in) rec.flags |= PREC_ROWS_COVER;
+        }
         if (g.spectral_model == MG_SPECTRUM_TABLE) {
           rec.clo = 0;
           rec.chi = G.nc - 1;

@@ -56,6 +56,7 @@ k_contract_fp32(Geo g, Ws w) {
   __shared__ __align__(16) float Ws_[F32_KC][TILE_PX];
   __shared__ __align__(16) float Ss_[F32_KC][CBLK];
   __shared__ PRec recs[F32_KC];
+  __shared__ int s_pid[F32_KC];
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ long long s_item;
 
@@ -95,12 +96,13 @@ k_contract_fp32(Geo g, Ws w) {
         if (tid < kn) {
           int pid = w.list[it.lbeg + k0 + tid];
           recs[tid] = w.rec[pid];
-          recs[tid].pad_ = pid;
+          s_pid[tid] = pid;
         } else {
           PRec z;
           z.ilo = 0; z.ihi = -1; z.jlo = 0; z.jhi = -1; z.clo = 1; z.chi = 0;
-          z.kslot = 0; z.pad_ = 0;
+          z.kslot = 0; z.flags = 0;
           recs[tid] = z;
+          s_pid[tid] = 0;
         }
       }
       __syncthreads();
@@ -121,7 +123,7 @@ k_contract_fp32(Geo g, Ws w) {
           float s = 0.f;
           if (c < nc && q < kn) {
             if (g.spectral_model == MG_SPECTRUM_TABLE) {
-              s = G.spectra[((long long)r.pad_ - G.p0) * nc + c];
+              s = G.spectra[((long long)s_pid[q] - G.p0) * nc + c];
             } else {
               s = channel_spectrum(r, g.spectral_model, c, dec, ehi, elo, inv_w);
             }

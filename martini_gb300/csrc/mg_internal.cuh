@@ -46,8 +46,14 @@ struct PRec {
   float vhi, vlo;          // velocity as a double-float pair, km/s
   float inv_s;             // 1 / (sqrt(2) sigma), km/s^-1
   float amp;               // mHI / D^2 / 2.36e5
-  int pad_;
+  int flags;               // PREC_* bits
 };
+
+// The footprint's rows [ilo, ihi] hold every cube row within the kernel's
+// support radius h of the particle (tested in FP64 with a 2^-20 margin, so
+// the FP32 profile argument of any other row is past the support): a radial
+// table kernel needs no per-row box test.
+constexpr int PREC_ROWS_COVER = 1;
 
 struct KSpec {
   int type;
@@ -304,6 +310,14 @@ constexpr float kPi = 3.14159265358979323846f;
 // a direct cell index, one float4 of coefficients and three FMAs, accurate
 // to ~1e-7 of f(0) in FP32 (7e-7 for Wendland C6) where the closed forms
 // lose up to 7e-4.
+// floor(u) and t = u - floor(u) for 0 <= u < 2^23 without conversions:
+// adding 2^23 rounded toward -inf leaves floor(u) in the low mantissa bits.
+__device__ __forceinline__ int kt_floor(float u, float& t) {
+  const float v = __fadd_rd(u, 8388608.f);
+  t = u - (v - 8388608.f);
+  return __float_as_int(v) - 0x4B000000;
+}
+
 __device__ __forceinline__ float kt_eval(int kt, float s) {
   const KTableInfo& inf = kt_info[kt];
   if (!(s < inf.smax)) return 0.f;
@@ -311,6 +325,13 @@ __device__ __forceinline__ float kt_eval(int kt, float s) {
   int r = 0;
   if (inf.nreg == 3) r = (s > 1.f) ? 2 : (R >= inf.split_r ? 1 : 0);
   const KRegion g = inf.reg[r];
+  if (g.var == 2) {  // cells in s; s >= smax lands on the zero cell
+    const float u = fminf(s * g.cells_per_unit, (float)g.ncell);
+    float t;
+    const int c = kt_floor(u, t);
+    const float4 cf = __ldg(reinterpret_cast<const float4*>(kt_coef) + g.first + c);
+    return fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
+  }
   const float a2 = fmaxf(1.f - s, 0.f);
   const float v = g.var ? (a2 > 0.f ? a2 * rsqrtf(a2) : 0.f) : R;
   const float u = (v - g.lo) * g.cells_per_unit;

