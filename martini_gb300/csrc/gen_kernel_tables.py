@@ -25,6 +25,7 @@ next to this file; the header is committed).
 
 from __future__ import annotations
 
+import math
 import os
 
 import numpy as np
@@ -204,6 +205,34 @@ def device_eval(regions, coefs, smax, s):
     return out
 
 
+# Truncation factor of the Gaussian kernel's pixel integral (sph_kernels.py
+# :1024-1031): erf(zmax / sqrt 2), zmax = sqrt(truncate^2 - q^2) in units of
+# sigma, on GT_NCELL cells over [0, GT_VMAX) and one cell holding 1 past it
+# (erf(8 / sqrt 2) is 1 in FP32).
+GT_VMAX = 8.0
+GT_NCELL = 256
+
+
+def f_trunc(v):
+    return np.array([math.erf(x / math.sqrt(2.0)) for x in np.atleast_1d(v)])
+
+
+def gauss_trunc_table():
+    co = np.vstack([fit_cells(f_trunc, 0.0, GT_VMAX, GT_NCELL),
+                    np.array([[1.0, 0.0, 0.0, 0.0]])]).astype(np.float32)
+    v = np.concatenate((np.linspace(0, 10, 200001), np.random.default_rng(1).uniform(0, 9, 100000)))
+    v32 = v.astype(np.float32)
+    u = np.minimum(v32 * np.float32(GT_NCELL / GT_VMAX), np.float32(GT_NCELL)).astype(np.float32)
+    c = np.floor(u).astype(np.int64)
+    t = (u - c.astype(np.float32)).astype(np.float32)
+    cf = co[c]
+    acc = cf[:, 3].copy()
+    for k in (2, 1, 0):
+        acc = (acc * t + cf[:, k]).astype(np.float32)
+    err = np.abs(acc - f_trunc(v32.astype(np.float64))).max()
+    return co, err
+
+
 def c_float(v):
     """A float literal of C: nine significant digits and a point or exponent."""
     t = f"{float(v):.9g}"
@@ -286,6 +315,17 @@ def main():
     body.append(f"__device__ __align__(16) const float kt_coef[{len(flat)}] = {{")
     for i in range(0, len(flat), DEG + 1):
         body.append("    " + ", ".join(c_float(v) for v in flat[i:i + DEG + 1]) + ",")
+    body.append("};")
+    body.append("")
+    gt, gt_err = gauss_trunc_table()
+    print("GAUSS_TRUNC", len(gt), f"{gt_err:.2e}")
+    hdr.append(f"//   Gaussian truncation factor erf(zmax / sqrt 2): {len(gt)} cells, "
+               f"FP32 max error {gt_err:.2e}")
+    body.append(f"constexpr int GT_NCELL = {GT_NCELL};  // cells of gt_coef before the cell of 1")
+    body.append(f"constexpr float GT_CELLS_PER_UNIT = {GT_NCELL / GT_VMAX!r}f;  // per unit zmax")
+    body.append(f"__device__ __align__(16) const float gt_coef[{gt.size}] = {{")
+    for row in gt:
+        body.append("    " + ", ".join(c_float(v) for v in row) + ",")
     body.append("};")
     body.append("")
     body.append("}  // namespace mg")

@@ -45,7 +45,7 @@ constexpr int KT_SMEM_CELLS = 1025;
 constexpr int TC_MASTER_COL = 256;
 // Shared memory at the widest band: two stages of A and B hi/lo tiles
 // (KC = 64) plus the static arrays must fit in the 227 KB of a CTA.
-static_assert(2 * (2 * 4 * 4096 + 2 * 4 * TC_MASTER_COL * 32) + KT_SMEM_CELLS * 16 +
+static_assert(2 * (2 * 4 * 4096 + 2 * 4 * TC_MASTER_COL * 32) + (KT_SMEM_CELLS + 257) * 16 +
                       2 * 64 * (sizeof(PRec) + sizeof(int) + sizeof(long long)) + 4096 <=
                   227 * 1024,
               "tensor-core kernel shared memory");
@@ -284,21 +284,6 @@ __device__ __forceinline__ void split_pair(float a, float b, unsigned& hi, unsig
   }
 }
 
-// GaussianKernel pixel integral (sph_kernels.py:994-1044), w_gaussian with
-// the per-particle quotients taken as products with reciprocals: the same
-// formula to an ulp or two, without six divisions per pixel.
-__device__ __forceinline__ float w_gaussian_tc(float dx, float dy, float inv_hs, float trunc,
-                                               float inv_gnorm) {
-  const float dr = sqrtf(dx * dx + dy * dy);
-  const float q = dr * inv_hs;
-  if ((dr - 0.70710678118654752f) * inv_hs > trunc) return 0.f;
-  const float zmax = trunc > q ? sqrtf(trunc * trunc - q * q) : 0.f;
-  const float s = inv_hs * 0.70710678118654752f;  // 1 / (h sqrt(2) sigma)
-  const float ex = erff((dx + 0.5f) * s) - erff((dx - 0.5f) * s);
-  const float ey = erff((dy + 0.5f) * s) - erff((dy - 0.5f) * s);
-  return 0.25f * erff(zmax * 0.70710678118654752f) * ex * ey * inv_gnorm;
-}
-
 // Coefficients of table cell floor(u) (u >= 0) from shared memory, and the
 // fraction t: base32 is the shared address of the table minus 2^23 cells,
 // so the sum of 2^23 and floor(u) left in the float's bits by kt_floor's
@@ -313,16 +298,70 @@ __device__ __forceinline__ float4 kt_cell_smem(unsigned base32, float u, float& 
   return c;
 }
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// GaussianKernel pixel integral (sph_kernels.py:994-1044) at the four
+// pixels of a lane,
+//   W = 0.25 erf(zmax / sqrt 2) (erf(x1) - erf(x0)) (erf(y1) - erf(y0)) / norm,
+// zmax = sqrt(truncate^2 - q^2) (0 past the truncation), q = dr / (h sigma).
+// The row factors of the tile's 8 rows come from lanes 0-7 and the column
+// factors of its 16 columns from lanes 8-23 (two erff each, shared by
+// shuffles); the truncation factor comes from its table in zmax (cubic cells,
+// ~6e-8).  Called by all 32 lanes.
+__device__ __forceinline__ void weights4_gauss(const PRec& r, const KSpec& kk, unsigned gtab_s32,
+                                               int ib, int j, int lane, float sw,
+                                               float (&w)[4]) {
+  const float inv_hs = 1.f / (r.h * 0.42466090014400953f);  // 1 / (h sigma_FWHM)
+  const float sc = inv_hs * 0.70710678118654752f;            // 1 / (h sqrt(2) sigma)
+  const int i0 = ib - (lane >> 4), j0 = j - (lane & 15);
+  const float d = lane < 8 ? (float)(r.xi - (i0 + lane)) + r.xf
+                           : (float)(r.yi - (j0 + ((lane - 8) & 15))) + r.yf;
+  const float e = erff((d + 0.5f) * sc) - erff((d - 0.5f) * sc);
+  const float ey = __shfl_sync(0xffffffffu, e, 8 + (lane & 15));
+  float ex[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) ex[k] = __shfl_sync(0xffffffffu, e, (lane >> 4) + 2 * k);
+  if (j < r.jlo || j > r.jhi) return;
+  const float dy = (float)(r.yi - j) + r.yf;
+  const float dy2 = dy * dy;
+  const float ihs2 = inv_hs * inv_hs;
+  const float t2 = kk.truncate * kk.truncate;
+  const float c = 0.25f / kk.gnorm * ey * sw;
+  const float dx0 = (float)(r.xi - ib) + r.xf;
+  const unsigned base32 = gtab_s32 - (0x4B000000u << 4);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = ib + 2 * k;
+    const float dxk = dx0 - (float)(2 * k);
+    const float z2 = fmaxf(fmaf(-fmaf(dxk, dxk, dy2), ihs2, t2), 0.f);  // truncate^2 - q^2
+    const float u = fminf(sqrt_approx(z2) * GT_CELLS_PER_UNIT, (float)GT_NCELL);
+    float t;
+    const float4 cf = kt_cell_smem(base32, u, t);
+    const float T = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
+    w[k] = (i >= r.ilo && i <= r.ihi) ? T * ex[k] * c : 0.f;
+  }
+}
+
 // W of one particle at the four pixels of a lane: rows ib + 2 k, column j.
 // ktab_s32 is the shared address of the launch's radial table (type
 // ktab_type, copied from its first cell); other radial types read kt_coef.
 __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec* ks,
                                          const float4* ktab, unsigned ktab_s32, int ktab_type,
-                                         int ib, int j, float sw, float (&w)[4]) {
+                                         unsigned gtab_s32, int ib, int j, int lane, float sw,
+                                         float (&w)[4]) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) w[k] = 0.f;
-  if (!valid || j < r.jlo || j > r.jhi) return;
+  if (!valid) return;  // warp-uniform
   const KSpec kk = ks[r.kslot];
+  if (kk.type == MG_KERNEL_GAUSSIAN) {  // warp-uniform; every lane takes part
+    weights4_gauss(r, kk, gtab_s32, ib, j, lane, sw, w);
+    return;
+  }
+  if (j < r.jlo || j > r.jhi) return;
   const float dy = (float)(r.yi - j) + r.yf;
   if (kk.type <= MG_KERNEL_QUARTIC_SPLINE && kk.type != MG_KERNEL_CUBIC_SPLINE) {
     // cells in s = R^2: the cell coordinate u = s * cells per unit s is
@@ -377,12 +416,6 @@ __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec*
   if (kk.type == MG_KERNEL_DIRAC) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) w[k] = in[k] ? sw : 0.f;
-  } else if (kk.type == MG_KERNEL_GAUSSIAN) {
-    const float inv_hs = 1.f / (r.h * 0.42466090014400953f);  // 1 / (h sigma_FWHM)
-    const float inv_gnorm = 1.f / kk.gnorm;
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      w[k] = in[k] ? w_gaussian_tc(dx[k], dy, inv_hs, kk.truncate, inv_gnorm) * sw : 0.f;
   } else {  // cubic spline: cells in R and A = sqrt(1 - R^2)
     const KTableInfo& inf = kt_info[kk.type];
     const float fac = 4.f * r.inv_h2;
@@ -402,15 +435,15 @@ __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec*
 template <bool BF16>
 __device__ __forceinline__ void produce_w_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
                                                const KSpec* ks, const float4* ktab,
-                                               unsigned ktab_s32, int ktab_type, int q, int i0,
-                                               int j0, int lane,
+                                               unsigned ktab_s32, int ktab_type,
+                                               unsigned gtab_s32, int q, int i0, int j0, int lane,
                                                float sw, unsigned char* a_hi,
                                                unsigned char* a_lo) {
   const int j = j0 + (lane & 15);
   const int ib = i0 + (lane >> 4);
   float w0[4], w1[4];
-  weights4(r0, v0, ks, ktab, ktab_s32, ktab_type, ib, j, sw, w0);
-  weights4(r1, v1, ks, ktab, ktab_s32, ktab_type, ib, j, sw, w1);
+  weights4(r0, v0, ks, ktab, ktab_s32, ktab_type, gtab_s32, ib, j, lane, sw, w0);
+  weights4(r1, v1, ks, ktab, ktab_s32, ktab_type, gtab_s32, ib, j, lane, sw, w1);
   // element (pixel p, particle q): K step q / 16, K core q / 8 % 2, (q % 8) * 2
   const unsigned qoff = (unsigned)(q >> 4) * 4096u + (unsigned)((q >> 3) & 1) * 128u +
                         (unsigned)(q & 7) * 2u;
@@ -620,6 +653,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   __shared__ long long s_soff[2][KC];  // spectrum store rows
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
+  __shared__ float4 s_gtab[GT_NCELL + 1];  // Gaussian truncation factor
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
@@ -642,6 +676,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   const unsigned sbase = smem_u32(smem);
 
   if (tid < MG_MAX_KERNELS) s_ks[tid] = g.ks[tid];
+  for (int e = tid; e < GT_NCELL + 1; e += TC_THREADS)
+    s_gtab[e] = reinterpret_cast<const float4*>(gt_coef)[e];
   // the table of the launch's radial kernel (at most one per kernel tuple)
   int ktab_type = -1;
   for (int k = 0; k < g.n_kernels; ++k)
@@ -835,8 +871,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
           pf2 = spec_at(spec, so0, r0, v0, wa + 32 + lane);
           pf3 = spec_at(spec, so1, r1, v1, wa + 32 + lane);
         }
-        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type, q,
-                             i0, j0, lane, sw, sa_hi, sa_lo);
+        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type,
+                             smem_u32(s_gtab), q, i0, j0, lane, sw, sa_hi, sa_lo);
         produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
                              w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
                              (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0), lane,
