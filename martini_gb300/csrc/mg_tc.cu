@@ -717,16 +717,23 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   int ncols = g.max_width;  // channels of the item's block held in TMEM (<= 256)
 
   const bool drain = ncols <= TC_MASTER_COL;  // master accumulator fits
-  auto zero_tmem = [&]() {
+  // Columns [lo, hi) of both accumulators that MMAs may have written since
+  // they were last zeroed (32-column chunk granularity, warp-uniform tests);
+  // TMEM is zero everywhere else.
+  auto chunk_in = [](int c, int lo, int hi) { return c < hi && c + 32 > lo; };
+  auto zero_tmem = [&](int lo, int hi) {
     for (int c = colgrp * 32; c < ncols; c += 128) {
+      if (!chunk_in(c, lo, hi)) continue;
       tmem_st32_zero(tmem + lane_base + c);
       if (drain) tmem_st32_zero(tmem + lane_base + TC_MASTER_COL + c);
     }
     tmem_wait_st();
   };
-  // master += working (round to nearest), working = 0; no MMA in flight
-  auto drain_tmem = [&]() {
+  // master += working (round to nearest), working = 0 over the columns
+  // written since the last drain; no MMA in flight
+  auto drain_tmem = [&](int lo, int hi) {
     for (int c = colgrp * 32; c < ncols; c += 128) {
+      if (!chunk_in(c, lo, hi)) continue;
       for (int h = 0; h < 32; h += 16) {
         unsigned a[16], b[16];
         tmem_ld16(tmem + lane_base + c + h, a);
@@ -743,7 +750,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     }
     tmem_wait_st();
   };
-  zero_tmem();
+  zero_tmem(0, ncols);
   tc_fence_before();
   __syncthreads();
 
@@ -779,6 +786,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     const float unscale = 1.f / (sw * ss);
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
     const int nchunk = (it.lcount + KC - 1) / KC;
+    int d_lo = 0x7fffffff, d_hi = 0;  // columns written since the last drain
+    int t_lo = 0x7fffffff, t_hi = 0;  // columns written by this item
 
     // records of the first stage
     if (tid < KC) {
@@ -842,6 +851,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         if (nw > nwmax) nw = nwmax;
         if (w0 + nw > ncols) w0 = ncols - nw;
         if (w0 < 0) w0 = 0;
+        d_lo = min(d_lo, w0);
+        d_hi = max(d_hi, w0 + nw);
+        t_lo = min(t_lo, w0);
+        t_hi = max(t_hi, w0 + nw);
       }
       unsigned char* const sa_hi = smem + stage * st_bytes;
       unsigned char* const sa_lo = sa_hi + a_bytes;
@@ -889,21 +902,23 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (s_abort) break;
       if (tid == 0) {
         tc_fence_after();
+        // nw <= nwmax <= 256: one MMA spans the window.  The descriptors'
+        // start-address field (bits 0-13, address / 16) steps by adding the
+        // K-step offsets: every stage address is below 256 KB, so no carry.
         const unsigned base = sbase + stage * st_bytes;
+        const unsigned id = idesc_f16kind(128, nw, BF16);
+        const unsigned long long a_hi = sdesc(base, 128, 256);
+        const unsigned long long a_lo = a_hi + (a_bytes >> 4);
+        const unsigned long long b_hi = sdesc(base + 2u * a_bytes, 128, 256);
+        const unsigned long long b_lo = b_hi + (b_bytes >> 4);
+        const unsigned bstep = (unsigned)nw * 2u;  // K step of B: nw * 32 bytes
+        const unsigned d = tmem + (unsigned)w0;
+#pragma unroll
         for (int ks = 0; ks < KSTEPS; ++ks) {
-          const unsigned a_hi = base + ks * 4096u;
-          const unsigned a_lo = a_hi + a_bytes;
-          for (int n0 = 0; n0 < nw; n0 += 256) {
-            const int pn = nw - n0 < 256 ? nw - n0 : 256;
-            const unsigned boff = ks * ((unsigned)nw * 32u) + (unsigned)(n0 >> 3) * 256u;
-            const unsigned b_hi = base + 2u * a_bytes + boff;
-            const unsigned b_lo = b_hi + b_bytes;
-            const unsigned d = tmem + (unsigned)(w0 + n0);
-            const unsigned id = idesc_f16kind(128, pn, BF16);
-            umma(d, sdesc(a_hi, 128, 256), sdesc(b_hi, 128, 256), id, 1u);
-            umma(d, sdesc(a_hi, 128, 256), sdesc(b_lo, 128, 256), id, 1u);
-            umma(d, sdesc(a_lo, 128, 256), sdesc(b_hi, 128, 256), id, 1u);
-          }
+          const unsigned ao = (unsigned)ks * 256u, bo = (unsigned)ks * bstep;
+          umma(d, a_hi + ao, b_hi + bo, id, 1u);
+          umma(d, a_hi + ao, b_lo + bo, id, 1u);
+          umma(d, a_lo + ao, b_hi + bo, id, 1u);
         }
         umma_commit(smem_u32(&bars[stage]));
       }
@@ -916,7 +931,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         phase_bits ^= 1u << s;
         pending_bits &= ~(1u << s);
         tc_fence_after();
-        drain_tmem();
+        drain_tmem(d_lo, d_hi);
+        d_lo = 0x7fffffff;
+        d_hi = 0;
         tc_fence_before();
         __syncthreads();
         since_drain = 0;
@@ -959,16 +976,23 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       }
       for (int c = colgrp * 32; c < ncols; c += 128) {
         unsigned r[32];
-        tmem_ld32(tmem + lane_base + (unsigned)c, r);
-        tmem_wait_ld();
-        if (drain) {
-          for (int h = 0; h < 32; h += 16) {
-            unsigned m[16];
-            tmem_ld16(tmem + lane_base + TC_MASTER_COL + (unsigned)(c + h), m);
-            tmem_wait_ld();
+        if (!chunk_in(c, t_lo, t_hi)) {
+          // never written: zero (already in a cleared or accumulated cube)
+          if (it.nk == 1) continue;
 #pragma unroll
-            for (int v = 0; v < 16; ++v)
-              r[h + v] = __float_as_uint(__uint_as_float(r[h + v]) + __uint_as_float(m[v]));
+          for (int v = 0; v < 32; ++v) r[v] = 0u;
+        } else {
+          tmem_ld32(tmem + lane_base + (unsigned)c, r);
+          tmem_wait_ld();
+          if (drain) {
+            for (int h = 0; h < 32; h += 16) {
+              unsigned m[16];
+              tmem_ld16(tmem + lane_base + TC_MASTER_COL + (unsigned)(c + h), m);
+              tmem_wait_ld();
+#pragma unroll
+              for (int v = 0; v < 16; ++v)
+                r[h + v] = __float_as_uint(__uint_as_float(r[h + v]) + __uint_as_float(m[v]));
+            }
           }
         }
         if (inside || it.nk != 1) {
@@ -1002,7 +1026,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         }
       }
     }
-    zero_tmem();
+    zero_tmem(t_lo, t_hi);
     tc_fence_before();
     __syncthreads();
   }
