@@ -340,8 +340,8 @@ int workspace_view(const Geo& g, void* ws, size_t bytes, long long cap_pairs,
   // the workspace beyond the fixed layout holds the spectrum store of the
   // tensor-core forms (Gaussian lines); without room they evaluate in-kernel
   if (tc_form(g.form) && g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
-    w->spec = reinterpret_cast<float*>(static_cast<char*>(ws) + L.total);
-    w->cap_spec = (long long)((bytes - L.total) / sizeof(float));
+    w->spec = reinterpret_cast<unsigned*>(static_cast<char*>(ws) + L.total);
+    w->cap_spec = (long long)((bytes - L.total) / sizeof(unsigned));
   }
   return MG_OK;
 }

@@ -202,7 +202,8 @@ struct Ws {
   long long* part_off;   // [nseg] exclusive scan of seg_part
   float* partial;        // [cap_partial_items][TILE_PX][max_width]
   double* flux_part;     // [nfpart]
-  float* spec;           // [cap_spec] per-particle Gaussian spectra over [clo, chi]
+  unsigned* spec;        // [cap_spec] per-particle Gaussian spectra over [clo, chi], as the
+                         // tensor-core form's scaled 16-bit hi | lo << 16 halves
   long long cap_spec;    // room in spec (the workspace beyond the fixed layout)
 };
 

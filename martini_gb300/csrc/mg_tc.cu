@@ -304,6 +304,23 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   return y;
 }
 
+// One value's 16-bit hi and lo halves packed as hi | lo << 16 (the same
+// roundings as split_pair).
+template <bool BF16>
+__device__ __forceinline__ unsigned split_one(float a) {
+  unsigned hi, lo;
+  split_pair<BF16>(a, 0.f, hi, lo);
+  return (hi & 0xFFFFu) | (lo << 16);
+}
+
+// Exact power-of-two scale of one cube's spectra in the FP16 split form:
+// the largest |S| bound -> 2^14.
+__device__ __forceinline__ float spec_scale(const GalState& gs, int model) {
+  const float sb = __uint_as_float(gs.sbound_bits) *
+                   (model == MG_SPECTRUM_TABLE ? 1.f : __uint_as_float(gs.invw_bits));
+  return sb > 0.f ? exp2f(14.f - ceilf(log2f(sb))) : 1.f;
+}
+
 // GaussianKernel pixel integral (sph_kernels.py:994-1044) at the four
 // pixels of a lane,
 //   W = 0.25 erf(zmax / sqrt 2) (erf(x1) - erf(x0)) (erf(y1) - erf(y0)) / norm,
@@ -493,9 +510,9 @@ __device__ __forceinline__ float half_diff_from_c(float ca, bool pa, float cb, b
 }
 
 // Spectrum store value of channel c for a particle (0 outside its support).
-__device__ __forceinline__ float spec_at(const float* spec, long long soff, const PRec& r, bool v,
-                                         int c) {
-  return (v && c >= r.clo && c <= r.chi) ? __ldg(spec + soff + (c - r.clo)) : 0.f;
+__device__ __forceinline__ unsigned spec_at(const unsigned* spec, long long soff, const PRec& r,
+                                           bool v, int c) {
+  return (v && c >= r.clo && c <= r.chi) ? __ldg(spec + soff + (c - r.clo)) : 0u;
 }
 
 // B = S for particles (q, q + 1) over the window channels.  A Gaussian line
@@ -508,19 +525,20 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
                                                const float* ehi, const float* elo,
                                                const float* inv_w, const float* spectra,
                                                int pid0, int pid1, int lane, float ss,
-                                               const float* spec, long long soff0,
-                                               long long soff1, float pf0, float pf1,
-                                               float pf2, float pf3, unsigned char* b_hi,
+                                               const unsigned* spec, long long soff0,
+                                               long long soff1, unsigned pf0, unsigned pf1,
+                                               unsigned pf2, unsigned pf3, unsigned char* b_hi,
                                                unsigned char* b_lo) {
   const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
                         (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
   if (spec) {
-    // Gaussian lines read from the spectrum store (rows over [clo, chi]);
-    // the first 64 window channels were loaded before the weights
+    // Gaussian lines read from the spectrum store, already scaled and split
+    // (hi | lo << 16 per value); the first 64 window channels were loaded
+    // before the weights
     for (int base = 0; base < nw; base += 32) {  // warp-uniform
       const int n = base + lane;
       const int c = w0 + n;
-      float s0, s1;
+      unsigned s0, s1;
       if (base == 0) {
         s0 = pf0;
         s1 = pf1;
@@ -531,14 +549,10 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
         s0 = spec_at(spec, soff0, r0, v0, c);
         s1 = spec_at(spec, soff1, r1, v1, c);
       }
-      s0 *= ss;
-      s1 *= ss;
       if (n < nw) {
         const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
-        unsigned hi, lo;
-        split_pair<BF16>(s0, s1, hi, lo);
-        *reinterpret_cast<unsigned*>(b_hi + off) = hi;
-        *reinterpret_cast<unsigned*>(b_lo + off) = lo;
+        *reinterpret_cast<unsigned*>(b_hi + off) = __byte_perm(s0, s1, 0x5410);
+        *reinterpret_cast<unsigned*>(b_lo + off) = __byte_perm(s0, s1, 0x7632);
       }
     }
     return;
@@ -608,6 +622,7 @@ __global__ void k_spec_count(Geo g, Ws w) {
 // the contraction gives the same bits with or without the store.  Row p
 // starts at pair_off[p] (exclusive scan of the row lengths).
 __global__ void k_spec_eval(Geo g, Ws w) {
+  const bool form_bf16 = g.form == MG_FORM_BF16X3;
   const bool fits = w.hdr->n_spec <= w.cap_spec;
   // read by the contraction, which runs after this whole kernel
   if (blockIdx.x == 0 && threadIdx.x == 0) w.hdr->spec_ready = fits ? 1 : 0;
@@ -626,7 +641,8 @@ __global__ void k_spec_eval(Geo g, Ws w) {
     const float* elo = w.elo + G.edge0;
     const float* inv_w = w.inv_w + G.edge0;
     const PRec r = w.rec[p];
-    float* out = w.spec + w.pair_off[p];
+    unsigned* out = w.spec + w.pair_off[p];
+    const float ss = form_bf16 ? 1.f : spec_scale(w.gst[gk], g.spectral_model);
     for (int base = 0; base < cnt; base += 31) {
       const int m = base + lane;
       const int c = r.clo + m;
@@ -637,7 +653,8 @@ __global__ void k_spec_eval(Geo g, Ws w) {
       const bool pb = __shfl_down_sync(0xffffffffu, (int)pa, 1) != 0;
       if (lane < 31 && m < cnt) {
         const float phi = dec ? half_diff_from_c(cb, pb, ca, pa) : half_diff_from_c(ca, pa, cb, pb);
-        out[m] = r.amp * inv_w[c] * phi;
+        out[m] = form_bf16 ? split_one<true>((r.amp * inv_w[c] * phi) * ss)
+                           : split_one<false>((r.amp * inv_w[c] * phi) * ss);
       }
     }
   }
@@ -665,7 +682,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   const long long n_items = w.hdr->n_items;
   const int kch = w.hdr->kch;
   // Gaussian lines come from the spectrum store when it was filled
-  const float* spec = (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 &&
+  const unsigned* spec = (g.spectral_model == MG_SPECTRUM_GAUSSIAN && w.cap_spec > 0 &&
                        w.hdr->spec_ready)
                           ? w.spec
                           : nullptr;
@@ -777,11 +794,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     float sw = 1.f, ss = 1.f;
     if (!BF16) {
       const float wb = __uint_as_float(gs.wbound_bits);
-      const float sb = __uint_as_float(gs.sbound_bits) *
-                       (g.spectral_model == MG_SPECTRUM_TABLE ? 1.f
-                                                              : __uint_as_float(gs.invw_bits));
       if (wb > 0.f) sw = exp2f(14.f - ceilf(log2f(wb)));
-      if (sb > 0.f) ss = exp2f(14.f - ceilf(log2f(sb)));
+      ss = spec_scale(gs, g.spectral_model);
     }
     const float unscale = 1.f / (sw * ss);
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
@@ -875,7 +889,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         const bool v1 = q + 1 < kn && r1.chi >= cb0 && r1.clo <= cb1;
         // spectrum store loads of the first 64 window channels, in flight
         // while the weights are computed
-        float pf0 = 0.f, pf1 = 0.f, pf2 = 0.f, pf3 = 0.f;
+        unsigned pf0 = 0u, pf1 = 0u, pf2 = 0u, pf3 = 0u;
         if (spec) {
           const long long so0 = s_soff[buf][q], so1 = s_soff[buf][q + 1];
           const int wa = it.c0 + w0;
