@@ -48,7 +48,7 @@ def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal
     tile scan (3), plan, emit, radix passes x (histogram, scan (3), scatter),
     segments, item and partial scans (2 x 3), partial check, [spectrum store:
     row lengths, scan (3), rows], [cube clear for batches], contraction,
-    split-K reduction, flux (2)."""
+    split-K reduction, flux (3)."""
     if ntiles is None:
         ntiles = ((nx + 7) // 8) * ((ny + 15) // 16)  # 8 x 16-pixel tiles
     bits = max(ntiles - 1, 0).bit_length() + max(nc - 1, 0).bit_length()
@@ -58,7 +58,7 @@ def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal
         n += 1 + 3 + 1
     if ngal > 1:
         n += 1
-    return n + 1 + 1 + 2
+    return n + 1 + 1 + 3
 
 
 def parse():

@@ -303,9 +303,26 @@ void launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s
   launch_reduce_partials(g, w, num_sms, s);
 }
 
-// FP64 flux sums of every cube of a batch: one block per unpadded pixel row
-// of all cubes (a thread per channel, voxels widened to FP64 and added in
-// row order), then one block per cube summing its rows in row order.
+// Double-float running sum (Knuth's TwoSum): hi carries the FP32 sum and lo
+// the rounding errors of its additions, so hi + lo is the sum to ~n eps^2
+// without FP64 arithmetic (FP64 units are few on this part).
+struct DFloat {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void df_add(DFloat& a, float x) {
+  const float t = __fadd_rn(a.hi, x);
+  const float bp = __fadd_rn(t, -a.hi);
+  const float e = __fadd_rn(__fadd_rn(a.hi, -__fadd_rn(t, -bp)), __fadd_rn(x, -bp));
+  a.hi = t;
+  a.lo = __fadd_rn(a.lo, e);
+}
+
+// Flux sums of every cube of a batch: one block per unpadded pixel row of
+// all cubes, a thread per channel adding the row's voxels in a fixed order
+// (four interleaved double-float sums, combined in FP64), then per cube one
+// thread per channel summing its rows in row order, and one block per cube
+// adding the channels.
 __global__ void k_flux_rows(Geo g, Ws w) {
   const int gk = find_gal(w.gr0, g.ngal, (int)blockIdx.x);
   const Gal& G = w.gal[gk];
@@ -313,26 +330,45 @@ __global__ void k_flux_rows(Geo g, Ws w) {
   const int r = blockIdx.x - G.row0;
   const int i = G.padx + r;
   const int nc = G.nc;
+  const int j1 = G.ny - G.pady;
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     const float* row = G.cube + ((long long)i * G.ny) * nc + c;
+    DFloat a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    int j = G.pady;
+    for (; j + 4 <= j1; j += 4) {
+      float x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = __ldcs(row + (long long)(j + u) * nc);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) df_add(a[u], x[u]);
+    }
+    for (; j < j1; ++j) df_add(a[0], __ldcs(row + (long long)j * nc));
     double acc = 0.0;
-    for (int j = G.pady; j < G.ny - G.pady; ++j) acc += (double)__ldcs(row + (long long)j * nc);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc += (double)a[u].hi + (double)a[u].lo;
     w.flux_part[G.fpart0 + (long long)r * nc + c] = acc;
   }
+}
+
+constexpr int FLUX_CH = 64;  // channels per block of k_flux_channels
+
+__global__ void k_flux_channels(Geo g, Ws w) {
+  const Gal& G = w.gal[blockIdx.y];
+  if (!G.flux) return;
+  const int c = blockIdx.x * FLUX_CH + threadIdx.x;
+  if (c >= G.nc) return;
+  const int rows = G.nx - 2 * G.padx;
+  double s = 0.0;
+  for (int r = 0; r < rows; ++r) s += w.flux_part[G.fpart0 + (long long)r * G.nc + c];
+  G.flux[1 + c] = s;
 }
 
 __global__ void k_flux_cubes(Geo g, Ws w) {
   __shared__ double red[256];
   const Gal& G = w.gal[blockIdx.x];
   if (!G.flux) return;
-  const int rows = G.nx - 2 * G.padx;
   double tot = 0.0;
-  for (int c = threadIdx.x; c < G.nc; c += blockDim.x) {
-    double s = 0.0;
-    for (int r = 0; r < rows; ++r) s += w.flux_part[G.fpart0 + (long long)r * G.nc + c];
-    G.flux[1 + c] = s;
-    tot += s;
-  }
+  for (int c = threadIdx.x; c < G.nc; c += blockDim.x) tot += G.flux[1 + c];
   red[threadIdx.x] = tot;
   __syncthreads();
   for (int off = blockDim.x / 2; off > 0; off >>= 1) {
@@ -346,6 +382,8 @@ void launch_flux_batch(const Geo& g, const Ws& w, cudaStream_t s) {
   if (g.nrows <= 0) return;
   const int thr = g.max_nc < 256 ? ((g.max_nc + 31) / 32) * 32 : 256;
   k_flux_rows<<<g.nrows, thr, 0, s>>>(g, w);
+  k_flux_channels<<<dim3((unsigned)((g.max_nc + FLUX_CH - 1) / FLUX_CH), (unsigned)g.ngal),
+                    FLUX_CH, 0, s>>>(g, w);
   k_flux_cubes<<<g.ngal, 256, 0, s>>>(g, w);
 }
 

@@ -621,6 +621,27 @@ __global__ void k_spec_count(Geo g, Ws w) {
 // one warp per particle, the same shared-edge arithmetic as the producer, so
 // the contraction gives the same bits with or without the store.  Row p
 // starts at pair_off[p] (exclusive scan of the row lengths).
+// What k_spec_eval needs of one particle (independent loads by index, so
+// the next particle's are in flight while this one's line is evaluated).
+struct SpecIn {
+  int cnt, clo;
+  long long off;
+  float vhi, vlo, inv_s, amp;
+};
+
+__device__ __forceinline__ SpecIn spec_in(const Ws& w, long long p) {
+  SpecIn q;
+  q.cnt = w.npairs[p];
+  q.off = w.pair_off[p];
+  const PRec& r = w.rec[p];
+  q.clo = r.clo;
+  q.vhi = r.vhi;
+  q.vlo = r.vlo;
+  q.inv_s = r.inv_s;
+  q.amp = r.amp;
+  return q;
+}
+
 __global__ void k_spec_eval(Geo g, Ws w) {
   const bool form_bf16 = g.form == MG_FORM_BF16X3;
   const bool fits = w.hdr->n_spec <= w.cap_spec;
@@ -629,34 +650,45 @@ __global__ void k_spec_eval(Geo g, Ws w) {
   if (!fits) return;
   const int lane = threadIdx.x & 31;
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; p < g.n;
-       p += nwarps) {
-    const int cnt = w.npairs[p];
-    if (cnt == 0) continue;  // warp-uniform
-    const int gk = find_gal(w.gp0, g.ngal, p);
-    const Gal& G = w.gal[gk];
-    const int dec = w.gst[gk].dec;
-    const int nc = G.nc;
-    const float* ehi = w.ehi + G.edge0;
-    const float* elo = w.elo + G.edge0;
-    const float* inv_w = w.inv_w + G.edge0;
-    const PRec r = w.rec[p];
-    unsigned* out = w.spec + w.pair_off[p];
-    const float ss = form_bf16 ? 1.f : spec_scale(w.gst[gk], g.spectral_model);
-    for (int base = 0; base < cnt; base += 31) {
-      const int m = base + lane;
-      const int c = r.clo + m;
-      float ca = 0.f;
-      bool pa = true;
-      if (m <= cnt && c <= nc) edge_term(r, c, ehi, elo, ca, pa);
-      const float cb = __shfl_down_sync(0xffffffffu, ca, 1);
-      const bool pb = __shfl_down_sync(0xffffffffu, (int)pa, 1) != 0;
-      if (lane < 31 && m < cnt) {
-        const float phi = dec ? half_diff_from_c(cb, pb, ca, pa) : half_diff_from_c(ca, pa, cb, pb);
-        out[m] = form_bf16 ? split_one<true>((r.amp * inv_w[c] * phi) * ss)
-                           : split_one<false>((r.amp * inv_w[c] * phi) * ss);
+  long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (p >= g.n) return;
+  SpecIn cur = spec_in(w, p);
+  for (; p < g.n; p += nwarps) {
+    const long long pn = p + nwarps;
+    SpecIn nxt;
+    if (pn < g.n) nxt = spec_in(w, pn);  // warp-uniform
+    if (cur.cnt > 0) {                    // warp-uniform
+      const int cnt = cur.cnt;
+      const int gk = find_gal(w.gp0, g.ngal, p);
+      const Gal& G = w.gal[gk];
+      const int dec = w.gst[gk].dec;
+      const int nc = G.nc;
+      const float* ehi = w.ehi + G.edge0;
+      const float* elo = w.elo + G.edge0;
+      const float* inv_w = w.inv_w + G.edge0;
+      PRec r;
+      r.vhi = cur.vhi;
+      r.vlo = cur.vlo;
+      r.inv_s = cur.inv_s;
+      unsigned* out = w.spec + cur.off;
+      const float ss = form_bf16 ? 1.f : spec_scale(w.gst[gk], g.spectral_model);
+      for (int base = 0; base < cnt; base += 31) {
+        const int m = base + lane;
+        const int c = cur.clo + m;
+        float ca = 0.f;
+        bool pa = true;
+        if (m <= cnt && c <= nc) edge_term(r, c, ehi, elo, ca, pa);
+        const float cb = __shfl_down_sync(0xffffffffu, ca, 1);
+        const bool pb = __shfl_down_sync(0xffffffffu, (int)pa, 1) != 0;
+        if (lane < 31 && m < cnt) {
+          const float phi =
+              dec ? half_diff_from_c(cb, pb, ca, pa) : half_diff_from_c(ca, pa, cb, pb);
+          out[m] = form_bf16 ? split_one<true>((cur.amp * inv_w[c] * phi) * ss)
+                             : split_one<false>((cur.amp * inv_w[c] * phi) * ss);
+        }
       }
     }
+    cur = nxt;
   }
 }
 
