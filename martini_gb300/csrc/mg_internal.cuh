@@ -260,26 +260,59 @@ __device__ __forceinline__ void box_bounds(double c, double r, int n, int& lo, i
   hi = h;
 }
 
-// Channel index range whose closed velocity interval meets [lo, hi].
+// Smallest k in [0, n] with pred(k) (pred monotone false -> true over
+// [0, n), pred(n) taken as true), searched from a guess: galloping steps to
+// bracket the answer, then bisection.  Exact for any guess; a right guess
+// costs two probes.
+template <class P>
+__device__ __forceinline__ int first_true(int n, int guess, P pred) {
+  int lo, hi;  // answer in (lo, hi]: pred(hi) true or hi == n, pred(lo) false or lo == -1
+  guess = min(max(guess, 0), n);
+  if (guess == n || pred(guess)) {
+    hi = guess;
+    int step = 1;
+    lo = guess - 1;
+    while (lo >= 0 && pred(lo)) {
+      hi = lo;
+      lo -= step;
+      step <<= 1;
+    }
+    if (lo < -1) lo = -1;
+  } else {
+    lo = guess;
+    int step = 1;
+    hi = guess + 1;
+    while (hi < n && !pred(hi)) {
+      lo = hi;
+      hi += step;
+      step <<= 1;
+    }
+    if (hi > n) hi = n;
+  }
+  while (hi - lo > 1) {
+    const int m = lo + ((hi - lo) >> 1);
+    if (pred(m)) hi = m; else lo = m;
+  }
+  return hi;
+}
+
+// Channel index range whose closed velocity interval meets [lo, hi].  The
+// FP64 edge comparisons decide; a linear guess from the end edges (exact
+// for uniform channels) starts each search.
 __device__ __forceinline__ void channel_range(const double* e, int nc, int dec, double lo,
                                               double hi, int& c0, int& c1) {
   // E(k) = edges in increasing order
   auto E = [&](int k) { return dec ? e[nc - k] : e[k]; };
-  // first c in [0, nc) with E(c + 1) >= lo
-  int a = 0, b = nc;
-  while (a < b) {
-    int m = (a + b) >> 1;
-    if (E(m + 1) >= lo) b = m; else a = m + 1;
-  }
-  int first = a;
+  const double e0 = E(0), en = E(nc);
+  const float scale = (float)nc / (float)(en - e0);
+  auto guess = [&](double v) {
+    const float t = floorf((float)(v - e0) * scale);
+    return t >= 0.f ? (t < (float)nc ? (int)t : nc) : 0;  // NaN -> 0
+  };
+  // first c in [0, nc) with E(c + 1) >= lo (nc if none)
+  const int first = first_true(nc, guess(lo) - 1, [&](int c) { return E(c + 1) >= lo; });
   // last c in [0, nc) with E(c) <= hi  ->  (first c with E(c) > hi) - 1
-  a = 0;
-  b = nc;
-  while (a < b) {
-    int m = (a + b) >> 1;
-    if (E(m) > hi) b = m; else a = m + 1;
-  }
-  int last = a - 1;
+  const int last = first_true(nc, guess(hi), [&](int c) { return E(c) > hi; }) - 1;
   if (first > last) {
     c0 = 1;
     c1 = 0;
@@ -293,7 +326,6 @@ __device__ __forceinline__ void channel_range(const double* e, int nc, int dec, 
     c1 = last;
   }
 }
-
 
 // ---------------------------------------------------------------------------
 // Kernel pixel integrals (martini/sph_kernels.py).  dx, dy are particle minus
