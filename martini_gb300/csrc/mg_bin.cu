@@ -351,11 +351,30 @@ __global__ void k_plan_finish(Geo g, Ws w, int num_sms) {
   }
 }
 
+// a / b for 0 <= a < 2^24, b >= 1, from a reciprocal estimate corrected to
+// the exact quotient.
+__device__ __forceinline__ int div_exact(int a, int b, float rb) {
+  int q = (int)(((float)a + 0.5f) * rb);
+  int r = a - q * b;
+  while (r < 0) {
+    --q;
+    r += b;
+  }
+  while (r >= b) {
+    ++q;
+    r -= b;
+  }
+  return q;
+}
+
 // Pairs in particle order: key = global segment << cbits | clo (one pair per
 // tile and channel block the particle's line meets), value = particle.  A
-// warp takes 32 particles and writes them one at a time with all its lanes,
-// so the stores of a particle's pairs are contiguous; each pair's position
-// pair_off[P] + e is the same as in a particle-per-thread loop.
+// warp takes 32 particles, whose pairs are one contiguous range of the
+// output (pair_off is the exclusive scan of the counts); each lane writes
+// every 32nd pair of the range, finding its particle by a search over the
+// lanes' first pairs, so every store of the warp is contiguous.  Pair e of
+// a particle enumerates its tiles row-major over (tx, ty), then its channel
+// blocks, at position pair_off[P] + e.
 __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict__ vals) {
   if (w.hdr->status & (ST_PAIRS | ST_EDGES)) return;
   const int lane = threadIdx.x & 31;
@@ -365,15 +384,15 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
     const long long P = base + lane;
     // this lane's particle: first pair, pair count and the parameters of its
     // tile / block ranges
-    long long o = 0;
+    long long o = 0x7fffffffffffffffll;  // lanes past the end never match
     int np = 0, tx0 = 0, ty0 = 0, nty_span = 1, cb0 = 0, nb = 1, clo = 0, seg0 = 0, nty = 1,
         ncb = 1;
     if (P < g.n) {
-      const PRec rec = w.rec[P];
-      if (rec.ilo <= rec.ihi) {
+      o = w.pair_off[P];
+      np = w.npairs[P];
+      if (np > 0) {
+        const PRec rec = w.rec[P];
         const Gal& G = w.gal[find_gal(w.gp0, g.ngal, P)];
-        o = w.pair_off[P];
-        np = w.npairs[P];
         tx0 = rec.ilo / TILE_I;
         ty0 = rec.jlo / TILE_J;
         nty_span = rec.jhi / TILE_J - ty0 + 1;
@@ -385,9 +404,19 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
         ncb = G.ncb;
       }
     }
-    for (int src = 0; src < 32; ++src) {
-      const int cnt = __shfl_sync(0xffffffffu, np, src);
-      if (cnt == 0) continue;  // warp-uniform
+    const int last = (int)min(31ll, g.n - 1 - base);
+    const long long start = __shfl_sync(0xffffffffu, o, 0);
+    const long long end = __shfl_sync(0xffffffffu, o + np, last);
+    for (long long f0 = start; f0 < end; f0 += 32) {  // warp-uniform
+      const long long f = f0 + lane;
+      // src = last lane whose first pair is <= f (offsets ascend over lanes;
+      // an empty particle shares its offset with the next one)
+      int src = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const long long ov = __shfl_sync(0xffffffffu, o, src + step);
+        if (ov <= f) src += step;
+      }
       const long long so = __shfl_sync(0xffffffffu, o, src);
       const int stx0 = __shfl_sync(0xffffffffu, tx0, src);
       const int sty0 = __shfl_sync(0xffffffffu, ty0, src);
@@ -398,15 +427,18 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
       const int sseg0 = __shfl_sync(0xffffffffu, seg0, src);
       const int snty = __shfl_sync(0xffffffffu, nty, src);
       const int sncb = __shfl_sync(0xffffffffu, ncb, src);
-      const int sp = (int)(base + src);
-      for (int e = lane; e < cnt; e += 32) {
-        // pair e: tiles row-major over (tx, ty), then the channel blocks
-        const int cb = scb0 + e % snb;
-        const int t = e / snb;
-        const int tx = stx0 + t / sspan, ty = sty0 + t % sspan;
+      if (f < end) {
+        const int e = (int)(f - so);
+        int t = e, cb = scb0;
+        if (snb > 1) {
+          t = div_exact(e, snb, __frcp_rn((float)snb));
+          cb = scb0 + (e - t * snb);
+        }
+        const int a = div_exact(t, sspan, __frcp_rn((float)sspan));
+        const int tx = stx0 + a, ty = sty0 + (t - a * sspan);
         const unsigned sg = (unsigned)(sseg0 + (tx * snty + ty) * sncb + cb);
-        keys[so + e] = (sg << g.cbits) | (unsigned)sclo;
-        vals[so + e] = sp;
+        keys[f] = (sg << g.cbits) | (unsigned)sclo;
+        vals[f] = (int)(base + src);
       }
     }
   }
