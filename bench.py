@@ -401,7 +401,8 @@ def main():
         pass
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     achieved_tf = flops / t_contract / 1e12
-    traffic = TRAFFIC_BYTES.get((a.workload, a.form))
+    # measured on the full workload only: no figure for a reduced particle count
+    traffic = TRAFFIC_BYTES.get((a.workload, a.form)) if a.n is None else None
     line = {
         "metric": METRIC,
         "value": cubes_per_s,
