@@ -320,9 +320,9 @@ __device__ __forceinline__ void df_add(DFloat& a, float x) {
 
 // Flux sums of every cube of a batch: one block per unpadded pixel row of
 // all cubes, a thread per channel adding the row's voxels in a fixed order
-// (four interleaved double-float sums, combined in FP64), then per cube one
-// thread per channel summing its rows in row order, and one block per cube
-// adding the channels.
+// (four interleaved double-float sums, combined in FP64), then per cube and
+// channel eight row groups (rows r = g mod 8) summed in FP64 and combined in
+// group order, and one block per cube adding the channels.
 __global__ void k_flux_rows(Geo g, Ws w) {
   const int gk = find_gal(w.gr0, g.ngal, (int)blockIdx.x);
   const Gal& G = w.gal[gk];
@@ -350,17 +350,27 @@ __global__ void k_flux_rows(Geo g, Ws w) {
   }
 }
 
-constexpr int FLUX_CH = 64;  // channels per block of k_flux_channels
+constexpr int FLUX_CH = 32;  // channels per block of k_flux_channels
+constexpr int FLUX_RG = 8;   // row groups per block: rows r = g (mod FLUX_RG)
 
-__global__ void k_flux_channels(Geo g, Ws w) {
+__global__ void __launch_bounds__(FLUX_CH * FLUX_RG) k_flux_channels(Geo g, Ws w) {
+  __shared__ double part[FLUX_RG][FLUX_CH];
   const Gal& G = w.gal[blockIdx.y];
   if (!G.flux) return;
-  const int c = blockIdx.x * FLUX_CH + threadIdx.x;
-  if (c >= G.nc) return;
+  const int cl = threadIdx.x % FLUX_CH, rg = threadIdx.x / FLUX_CH;
+  const int c = blockIdx.x * FLUX_CH + cl;
   const int rows = G.nx - 2 * G.padx;
   double s = 0.0;
-  for (int r = 0; r < rows; ++r) s += w.flux_part[G.fpart0 + (long long)r * G.nc + c];
-  G.flux[1 + c] = s;
+  if (c < G.nc)
+    for (int r = rg; r < rows; r += FLUX_RG) s += w.flux_part[G.fpart0 + (long long)r * G.nc + c];
+  part[rg][cl] = s;
+  __syncthreads();
+  if (rg == 0 && c < G.nc) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < FLUX_RG; ++k) t += part[k][cl];
+    G.flux[1 + c] = t;
+  }
 }
 
 __global__ void k_flux_cubes(Geo g, Ws w) {
@@ -383,7 +393,7 @@ void launch_flux_batch(const Geo& g, const Ws& w, cudaStream_t s) {
   const int thr = g.max_nc < 256 ? ((g.max_nc + 31) / 32) * 32 : 256;
   k_flux_rows<<<g.nrows, thr, 0, s>>>(g, w);
   k_flux_channels<<<dim3((unsigned)((g.max_nc + FLUX_CH - 1) / FLUX_CH), (unsigned)g.ngal),
-                    FLUX_CH, 0, s>>>(g, w);
+                    FLUX_CH * FLUX_RG, 0, s>>>(g, w);
   k_flux_cubes<<<g.ngal, 256, 0, s>>>(g, w);
 }
 
