@@ -77,6 +77,25 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
   return false;
 }
 
+// 8-byte asynchronous global -> shared copies (both addresses 8-byte aligned).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
+               : "memory");
+}
+// one particle record (72 bytes: nine 8-byte pieces)
+__device__ __forceinline__ void cp_async_rec(void* dst, const void* src) {
+  static_assert(sizeof(PRec) % 8 == 0, "records copy in 8-byte pieces");
+#pragma unroll
+  for (int k = 0; k < (int)(sizeof(PRec) / 8); ++k)
+    cp_async8(static_cast<char*>(dst) + 8 * k, static_cast<const char*>(src) + 8 * k);
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -697,7 +716,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
   constexpr int KSTEPS = KC / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ PRec recs[2][KC];
+  __shared__ __align__(16) PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
   __shared__ long long s_soff[2][KC];  // spectrum store rows
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
@@ -835,7 +854,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     int d_lo = 0x7fffffff, d_hi = 0;  // columns written since the last drain
     int t_lo = 0x7fffffff, t_hi = 0;  // columns written by this item
 
-    // records of the first stage
+    // records of the first stage; the list entry of the second
+    int pid_ahead = 0;
     if (tid < KC) {
       if (tid < it.lcount) {
         const int pid = w.list[it.lbeg + tid];
@@ -847,6 +867,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         s_pid[0][tid] = 0;
         s_soff[0][tid] = 0;
       }
+      if (KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + KC + tid];
     }
     __syncthreads();
 
@@ -860,19 +881,24 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         phase_bits ^= 1u << stage;
         pending_bits &= ~(1u << stage);
       }
-      // fetch the next stage's records while this one is produced
-      PRec nrec;
-      int npid = 0;
-      long long nsoff = 0;
+      // the next stage's records travel global -> shared by cp.async while
+      // this one is produced (its list entry was read a stage earlier); the
+      // list entry of the stage after is read now
       const bool has_next = ch + 1 < nchunk;
       if (has_next && tid < KC) {
         if (k0 + KC + tid < it.lcount) {
-          npid = w.list[it.lbeg + k0 + KC + tid];
-          nrec = w.rec[npid];
-          if (spec) nsoff = w.pair_off[npid];
+          const int npid = pid_ahead;
+          cp_async_rec(&recs[buf ^ 1][tid], w.rec + npid);
+          if (spec) cp_async8(&s_soff[buf ^ 1][tid], w.pair_off + npid);
+          else s_soff[buf ^ 1][tid] = 0;
+          s_pid[buf ^ 1][tid] = npid;
         } else {
-          nrec = empty_rec();
+          recs[buf ^ 1][tid] = empty_rec();
+          s_pid[buf ^ 1][tid] = 0;
+          s_soff[buf ^ 1][tid] = 0;
         }
+        cp_async_commit();
+        if (k0 + 2 * KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + tid];
       }
       // stage channel window [w0, w0 + nw): min clo, max chi (every warp)
       int w0, nw;
@@ -938,11 +964,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
                              ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf0, pf1, pf2, pf3, sb_hi,
                              sb_lo);
       }
-      if (has_next && tid < KC) {
-        recs[buf ^ 1][tid] = nrec;
-        s_pid[buf ^ 1][tid] = npid;
-        s_soff[buf ^ 1][tid] = nsoff;
-      }
+      if (has_next && tid < KC) cp_async_wait_all();
       fence_proxy_async();
       __syncthreads();
       if (s_abort) break;
