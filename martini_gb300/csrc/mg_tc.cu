@@ -852,6 +852,11 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
     const int nchunk = (it.lcount + KC - 1) / KC;
     int d_lo = 0x7fffffff, d_hi = 0;  // columns written since the last drain
+    // a drain scheduled after a stage's MMAs runs halfway through the next
+    // stage's production, when those MMAs have completed (no MMA of the next
+    // stage is issued before its barrier), over columns [p_lo, p_hi)
+    bool drain_due = false;
+    int p_lo = 0, p_hi = 0;
     int t_lo = 0x7fffffff, t_hi = 0;  // columns written by this item
 
     // records of the first stage; the list entry of the second
@@ -937,6 +942,16 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       constexpr int PPW = KC / (TC_THREADS / 32);
 #pragma unroll
       for (int pp = 0; pp < PPW; pp += 2) {
+        if (pp == PPW / 2 && drain_due) {  // warp-uniform
+          const int sp = stage ^ 1;  // the previous stage's buffer
+          if (!mbar_wait(smem_u32(&bars[sp]), (phase_bits >> sp) & 1u)) s_abort = 1;
+          phase_bits ^= 1u << sp;
+          pending_bits &= ~(1u << sp);
+          tc_fence_after();
+          drain_tmem(p_lo, p_hi);
+          tc_fence_before();
+          drain_due = false;
+        }
         const int q = warp * PPW + pp;
         const PRec r0 = recs[buf][q];
         const PRec r1 = recs[buf][q + 1];
@@ -993,19 +1008,14 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       pending_bits |= 1u << stage;
       stage ^= 1;
       if (drain && ++since_drain == TC_DRAIN && ch + 1 < nchunk) {
-        // wait for this stage's MMAs (the commit covers all earlier ones)
-        const int s = stage ^ 1;
-        if (!mbar_wait(smem_u32(&bars[s]), (phase_bits >> s) & 1u)) s_abort = 1;
-        phase_bits ^= 1u << s;
-        pending_bits &= ~(1u << s);
-        tc_fence_after();
-        drain_tmem(d_lo, d_hi);
+        // drain the interval's columns during the next stage (its commit
+        // covers every earlier MMA)
+        drain_due = true;
+        p_lo = d_lo;
+        p_hi = d_hi;
         d_lo = 0x7fffffff;
         d_hi = 0;
-        tc_fence_before();
-        __syncthreads();
         since_drain = 0;
-        if (s_abort) break;
       }
     }
     since_drain = 0;
