@@ -711,13 +711,31 @@ __global__ void k_spec_eval(Geo g, Ws w) {
   }
 }
 
+// Min clo and max chi over the records of one warp's 32 particles of a
+// stage (invalid entries ignored), written by lane 0 to win[warp].
+__device__ __forceinline__ void window_partial(int (*win)[2], const PRec& r, bool valid, int warp,
+                                               int lane) {
+  int lo = valid ? r.clo : 0x7fffffff, hi = valid ? r.chi : -1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) {
+    win[warp][0] = lo;
+    win[warp][1] = hi;
+  }
+}
+
 template <bool BF16, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
+  static_assert(KC == 64, "records of a stage: warps 0 and 1, one per thread");
   constexpr int KSTEPS = KC / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(16) PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
+  __shared__ int s_win[2][2][2];  // [stage buffer][warp 0, 1][min clo, max chi]
   __shared__ long long s_soff[2][KC];  // spectrum store rows
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
@@ -873,6 +891,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         s_soff[0][tid] = 0;
       }
       if (KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + KC + tid];
+      window_partial(s_win[0], recs[0][tid], tid < it.lcount, warp, lane);
     }
     __syncthreads();
 
@@ -905,19 +924,13 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         cp_async_commit();
         if (k0 + 2 * KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + tid];
       }
-      // stage channel window [w0, w0 + nw): min clo, max chi (every warp)
+      // stage channel window [w0, w0 + nw): min clo, max chi
       int w0, nw;
       {
-        int lo = 0x7fffffff, hi = -1;
-        for (int q = lane; q < kn; q += 32) {
-          lo = min(lo, recs[buf][q].clo);
-          hi = max(hi, recs[buf][q].chi);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-          hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        }
+        // the two halves' extremes, reduced by warps 0 and 1 when the
+        // records arrived
+        int lo = min(s_win[buf][0][0], s_win[buf][1][0]);
+        int hi = max(s_win[buf][0][1], s_win[buf][1][1]);
         // relative to the segment's block [c0, c0 + ncols)
         lo = max(lo, it.c0) - it.c0;
         hi = min(hi, it.c0 + ncols - 1) - it.c0;
@@ -979,7 +992,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
                              ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf0, pf1, pf2, pf3, sb_hi,
                              sb_lo);
       }
-      if (has_next && tid < KC) cp_async_wait_all();
+      if (has_next && tid < KC) {
+        cp_async_wait_all();
+        window_partial(s_win[buf ^ 1], recs[buf ^ 1][tid], k0 + KC + tid < it.lcount, warp, lane);
+      }
       fence_proxy_async();
       __syncthreads();
       if (s_abort) break;
