@@ -143,52 +143,28 @@ __global__ void k_radix_hist(const unsigned* __restrict__ keys, const long long*
   }
 }
 
-// Ranks as in a stable per-element scatter, but each tile is first placed in
-// shared memory in digit order (tile digit starts from the tile histogram),
-// then written out run by run, so consecutive threads store consecutive
-// output positions.
-__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
-    const unsigned* __restrict__ kin, const int* __restrict__ vin, unsigned* __restrict__ kout,
-    int* __restrict__ vout, const long long* __restrict__ np, long long cap, int shift,
-    const int* __restrict__ hist, const long long* __restrict__ off, long long nblocks_cap) {
-  __shared__ unsigned s_key[RS_TILE];
-  __shared__ int s_val[RS_TILE];
+__global__ void k_radix_scatter(const unsigned* __restrict__ kin, const int* __restrict__ vin,
+                                unsigned* __restrict__ kout, int* __restrict__ vout,
+                                const long long* __restrict__ np, long long cap, int shift,
+                                const long long* __restrict__ off, long long nblocks_cap) {
   __shared__ int running[256];
   __shared__ int wcnt[RS_WARPS][256];
-  __shared__ int tstart[256];
-  __shared__ int wsum[RS_WARPS];
   __shared__ long long base_off[256];
   const long long n = min(*np, cap);
   const long long nb = (n + RS_TILE - 1) / RS_TILE;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (long long b = blockIdx.x; b < nb; b += gridDim.x) {
-    // digit starts within the tile: exclusive scan of its histogram
-    {
-      const int cnt = hist[(long long)threadIdx.x * nblocks_cap + b];
-      int incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      if (lane == 31) wsum[warp] = incl;
-      running[threadIdx.x] = 0;
-      base_off[threadIdx.x] = off[(long long)threadIdx.x * nblocks_cap + b];
-      for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
-      __syncthreads();
-      int before = 0;
-      for (int w = 0; w < warp; ++w) before += wsum[w];
-      tstart[threadIdx.x] = before + incl - cnt;
-      __syncthreads();
-    }
+    running[threadIdx.x] = 0;
+    base_off[threadIdx.x] = off[(long long)threadIdx.x * nblocks_cap + b];
+    for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
     const long long base = b * RS_TILE;
-    const int tn = (int)min((long long)RS_TILE, n - base);
     for (int r = 0; r < RS_ROUNDS; ++r) {
       const long long i = base + r * RS_THREADS + threadIdx.x;
       const bool valid = i < n;
-      const unsigned key = valid ? kin[i] : 0u;
-      const int val = valid ? vin[i] : 0;
-      // invalid lanes get digit 256 (never placed)
+      unsigned key = valid ? kin[i] : 0u;
+      int val = valid ? vin[i] : 0;
+      // invalid lanes get digit 256 (never written)
       const int digit = valid ? (int)((key >> shift) & 255u) : 256;
       const unsigned peers = __match_any_sync(0xffffffffu, digit);
       const int rank_in_warp = __popc(peers & ((1u << lane) - 1u));
@@ -198,9 +174,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
       if (valid) {
         int before = running[digit];
         for (int w = 0; w < warp; ++w) before += wcnt[w][digit];
-        const int pos = tstart[digit] + before + rank_in_warp;
-        s_key[pos] = key;
-        s_val[pos] = val;
+        const long long dst = base_off[digit] + before + rank_in_warp;
+        kout[dst] = key;
+        vout[dst] = val;
       }
       __syncthreads();
       {
@@ -213,14 +189,6 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
       }
       __syncthreads();
     }
-    for (int t = threadIdx.x; t < tn; t += RS_THREADS) {
-      const unsigned key = s_key[t];
-      const int digit = (int)((key >> shift) & 255u);
-      const long long dst = base_off[digit] + (t - tstart[digit]);
-      kout[dst] = key;
-      vout[dst] = s_val[t];
-    }
-    __syncthreads();
   }
 }
 
@@ -243,8 +211,7 @@ bool launch_radix_sort(unsigned* keys, int* vals, unsigned* kt, int* vt, const l
     const int shift = 8 * p;
     k_radix_hist<<<(unsigned)grid, RS_THREADS, 0, s>>>(ki, np, cap, shift, hist, nbc);
     launch_scan(hist, 256 * nbc, off, sums, nullptr, s);
-    k_radix_scatter<<<(unsigned)grid, RS_THREADS, 0, s>>>(ki, vi, ko, vo, np, cap, shift, hist,
-                                                          off, nbc);
+    k_radix_scatter<<<(unsigned)grid, RS_THREADS, 0, s>>>(ki, vi, ko, vo, np, cap, shift, off, nbc);
     unsigned* tk = ki; ki = ko; ko = tk;
     int* tv = vi; vi = vo; vo = tv;
   }
