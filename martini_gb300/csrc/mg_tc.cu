@@ -672,25 +672,35 @@ __global__ void k_spec_eval(Geo g, Ws w) {
   long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   if (p >= g.n) return;
   SpecIn cur = spec_in(w, p);
+  // the cube of the warp's particles: its edges, direction and scale, reloaded
+  // only when the cube changes (a cube's particles are contiguous and p only
+  // grows)
+  int gk_c = -1, dec = 0, nc = 0;
+  long long gp1 = -1;  // first particle past cube gk_c
+  const float *ehi = nullptr, *elo = nullptr, *inv_w = nullptr;
+  float ss = 1.f;
   for (; p < g.n; p += nwarps) {
     const long long pn = p + nwarps;
     SpecIn nxt;
     if (pn < g.n) nxt = spec_in(w, pn);  // warp-uniform
     if (cur.cnt > 0) {                    // warp-uniform
       const int cnt = cur.cnt;
-      const int gk = find_gal(w.gp0, g.ngal, p);
-      const Gal& G = w.gal[gk];
-      const int dec = w.gst[gk].dec;
-      const int nc = G.nc;
-      const float* ehi = w.ehi + G.edge0;
-      const float* elo = w.elo + G.edge0;
-      const float* inv_w = w.inv_w + G.edge0;
+      if (gk_c < 0 || p >= gp1) {
+        gk_c = find_gal(w.gp0, g.ngal, p);
+        const Gal& G = w.gal[gk_c];
+        gp1 = w.gp0[gk_c + 1];
+        dec = w.gst[gk_c].dec;
+        nc = G.nc;
+        ehi = w.ehi + G.edge0;
+        elo = w.elo + G.edge0;
+        inv_w = w.inv_w + G.edge0;
+        ss = form_bf16 ? 1.f : spec_scale(w.gst[gk_c], g.spectral_model);
+      }
       PRec r;
       r.vhi = cur.vhi;
       r.vlo = cur.vlo;
       r.inv_s = cur.inv_s;
       unsigned* out = w.spec + cur.off;
-      const float ss = form_bf16 ? 1.f : spec_scale(w.gst[gk], g.spectral_model);
       for (int base = 0; base < cnt; base += 31) {
         const int m = base + lane;
         const int c = cur.clo + m;
