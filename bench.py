@@ -38,7 +38,7 @@ L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) of one launch of the contraction kernel, from
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the full workload;
 # profiles/k_contract_tc_disc1m_512_f16x3.md gives the command and figures
-TRAFFIC_BYTES = {("disc1m_512", "f16x3"): 2_890_988_800}
+TRAFFIC_BYTES = {("disc1m_512", "f16x3"): 2_895_373_312}
 
 
 def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal: int = 1,
