@@ -302,8 +302,10 @@ int mg_check(void* workspace, void* stream);
 int mg_spectra(const mg_problem* p, float* out, void* stream);
 
 /*
- * FP64 flux sums of a cube already in device memory: flux[0] = total over
- * the unpadded region, flux[1 + c] = per channel (martini/martini.py:367-392).
+ * Flux sums of a cube already in device memory, returned in FP64 (each
+ * pixel row summed in double-float, rows and channels in FP64, in a fixed
+ * order): flux[0] = total over the unpadded region, flux[1 + c] = per
+ * channel (martini/martini.py:367-392).
  */
 int mg_flux(const float* cube, int32_t nx, int32_t ny, int32_t nc, int32_t padx,
             int32_t pady, double* flux, void* workspace, size_t workspace_bytes,

@@ -244,11 +244,45 @@ void launch_reduce_partials(const Geo& g, const Ws& w, int num_sms, cudaStream_t
   k_reduce_partials<<<num_sms * 8, RED_THREADS, 0, s>>>(g, w);
 }
 
-// FP64 flux sums over the unpadded region (martini/martini.py:367-392):
-// every voxel is widened to FP64 and added in a fixed order, per pixel row
-// (one block per row of the unpadded region, a thread per channel), then
-// the row sums in row order.
+// Flux sums over the unpadded region (martini/martini.py:367-392), in a
+// fixed order: per pixel row (one block per row of the unpadded region, a
+// thread per channel) in double-float, then the row sums in FP64 in row
+// order.
 constexpr int FLUX_ROWS = 1;  // pixel rows (axis 0) per chunk
+
+// Double-float running sum (Knuth's TwoSum): hi carries the FP32 sum and lo
+// the rounding errors of its additions, so hi + lo is the sum to ~n eps^2
+// without FP64 arithmetic (FP64 units are few on this part).
+struct DFloat {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void df_add(DFloat& a, float x) {
+  const float t = __fadd_rn(a.hi, x);
+  const float bp = __fadd_rn(t, -a.hi);
+  const float e = __fadd_rn(__fadd_rn(a.hi, -__fadd_rn(t, -bp)), __fadd_rn(x, -bp));
+  a.hi = t;
+  a.lo = __fadd_rn(a.lo, e);
+}
+
+// Sum of one pixel row's voxels of channel c (stride nc), j in [j0, j1), in
+// a fixed order: four interleaved double-float sums combined in FP64.
+__device__ __forceinline__ double row_sum(const float* row, int j0, int j1, int nc) {
+  DFloat a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  int j = j0;
+  for (; j + 4 <= j1; j += 4) {
+    float x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = __ldcs(row + (long long)(j + u) * nc);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) df_add(a[u], x[u]);
+  }
+  for (; j < j1; ++j) df_add(a[0], __ldcs(row + (long long)j * nc));
+  double acc = 0.0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) acc += (double)a[u].hi + (double)a[u].lo;
+  return acc;
+}
 
 __global__ void k_flux_partial(const float* __restrict__ cube, int nx, int ny, int nc, int padx,
                                int pady, double* __restrict__ part) {
@@ -257,10 +291,7 @@ __global__ void k_flux_partial(const float* __restrict__ cube, int nx, int ny, i
   const int i1 = min(nx - padx, i0 + FLUX_ROWS);
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     double acc = 0.0;
-    for (int i = i0; i < i1; ++i) {
-      const float* row = cube + ((long long)i * ny) * nc + c;
-      for (int j = pady; j < ny - pady; ++j) acc += (double)__ldcs(row + (long long)j * nc);
-    }
+    for (int i = i0; i < i1; ++i) acc += row_sum(cube + ((long long)i * ny) * nc + c, pady, ny - pady, nc);
     part[(long long)chunk * nc + c] = acc;
   }
 }
@@ -303,21 +334,6 @@ void launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s
   launch_reduce_partials(g, w, num_sms, s);
 }
 
-// Double-float running sum (Knuth's TwoSum): hi carries the FP32 sum and lo
-// the rounding errors of its additions, so hi + lo is the sum to ~n eps^2
-// without FP64 arithmetic (FP64 units are few on this part).
-struct DFloat {
-  float hi, lo;
-};
-
-__device__ __forceinline__ void df_add(DFloat& a, float x) {
-  const float t = __fadd_rn(a.hi, x);
-  const float bp = __fadd_rn(t, -a.hi);
-  const float e = __fadd_rn(__fadd_rn(a.hi, -__fadd_rn(t, -bp)), __fadd_rn(x, -bp));
-  a.hi = t;
-  a.lo = __fadd_rn(a.lo, e);
-}
-
 // Flux sums of every cube of a batch: one block per unpadded pixel row of
 // all cubes, a thread per channel adding the row's voxels in a fixed order
 // (four interleaved double-float sums, combined in FP64), then per cube and
@@ -331,23 +347,9 @@ __global__ void k_flux_rows(Geo g, Ws w) {
   const int i = G.padx + r;
   const int nc = G.nc;
   const int j1 = G.ny - G.pady;
-  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-    const float* row = G.cube + ((long long)i * G.ny) * nc + c;
-    DFloat a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    int j = G.pady;
-    for (; j + 4 <= j1; j += 4) {
-      float x[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) x[u] = __ldcs(row + (long long)(j + u) * nc);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) df_add(a[u], x[u]);
-    }
-    for (; j < j1; ++j) df_add(a[0], __ldcs(row + (long long)j * nc));
-    double acc = 0.0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) acc += (double)a[u].hi + (double)a[u].lo;
-    w.flux_part[G.fpart0 + (long long)r * nc + c] = acc;
-  }
+  for (int c = threadIdx.x; c < nc; c += blockDim.x)
+    w.flux_part[G.fpart0 + (long long)r * nc + c] =
+        row_sum(G.cube + ((long long)i * G.ny) * nc + c, G.pady, j1, nc);
 }
 
 constexpr int FLUX_CH = 32;  // channels per block of k_flux_channels
