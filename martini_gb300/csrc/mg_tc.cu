@@ -14,9 +14,12 @@
 // channels), at the stage's column window.  Two shared-memory stages
 // alternate: producers fill one while the tensor core reads the other, and
 // tcgen05.commit arrives on the stage's mbarrier when it may be reused.  The
-// records of the next stage are fetched while the current one is produced.
-// The epilogue reads TMEM with tcgen05.ld and writes 128-byte channel runs
-// of each pixel to the cube, or to a split-K partial buffer.
+// records of the next stage travel global -> shared by cp.async while the
+// current one is produced.  Every two stages the working accumulator is
+// drained (round to nearest) into a master accumulator in the other half of
+// TMEM, halfway through the next stage's production.  The epilogue reads
+// TMEM with tcgen05.ld and writes 128-byte channel runs of each pixel to the
+// cube, or to a split-K partial buffer.
 //
 // Every mbarrier wait has an iteration limit: on expiry the kernel sets
 // ST_TIMEOUT, frees its TMEM and returns.
