@@ -241,7 +241,10 @@ def c_float(v):
     return t + "f"
 
 
-def main():
+def render(verbose: bool = False):
+    """The header text and the emulated FP32 error of each table (relative
+    to f(0) for the kernel profiles, absolute for the truncation factor)."""
+    errors = {}
     rng = np.random.default_rng(0)
     hdr = [
         "// Generated by gen_kernel_tables.py -- do not edit.",
@@ -267,7 +270,9 @@ def main():
         err = np.abs(device_eval(regions, coefs, smax, s)
                      - f(np.minimum(s.astype(np.float32).astype(np.float64), 2 * smax))).max() / f0
         hdr.append(f"//   {name}: {len(coefs)} cells, FP32 device-form max error {err:.2e} of f(0)")
-        print(name, len(coefs), f"{err:.2e}")
+        errors[name] = err
+        if verbose:
+            print(name, len(coefs), f"{err:.2e}")
         regs = []
         first = ncoef_cells
         for (var, lo, hi, n), cells in zip(regions, region_cells(regions)):
@@ -318,7 +323,9 @@ def main():
     body.append("};")
     body.append("")
     gt, gt_err = gauss_trunc_table()
-    print("GAUSS_TRUNC", len(gt), f"{gt_err:.2e}")
+    errors["GAUSS_TRUNC"] = gt_err
+    if verbose:
+        print("GAUSS_TRUNC", len(gt), f"{gt_err:.2e}")
     hdr.append(f"//   Gaussian truncation factor erf(zmax / sqrt 2): {len(gt)} cells, "
                f"FP32 max error {gt_err:.2e}")
     body.append(f"constexpr int GT_NCELL = {GT_NCELL};  // cells of gt_coef before the cell of 1")
@@ -330,9 +337,16 @@ def main():
     body.append("")
     body.append("}  // namespace mg")
     body.append("")
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mg_kernel_tables.h")
-    with open(path, "w") as fh:
-        fh.write("\n".join(hdr + body))
+    return "\n".join(hdr + body), errors
+
+
+HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mg_kernel_tables.h")
+
+
+def main():
+    text, _ = render(verbose=True)
+    with open(HEADER, "w") as fh:
+        fh.write(text)
 
 
 if __name__ == "__main__":
