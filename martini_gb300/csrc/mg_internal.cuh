@@ -232,6 +232,33 @@ int flux_chunks(int nx, int padx);
 
 // Footprint and channel support (FP64), shared by the binning and the
 // global-profile kernels.
+// |k - c| <= r as the reference evaluates it, in FP64.  For moderate
+// coordinates (m = |c| + r + 1 < 1e6, k within r + 2 of c) the FP32
+// difference decides whenever it clears r by 4e-7 m: c and r rounded to FP32
+// and the FP32 subtraction are each off by at most 2^-24 of their magnitude,
+// about 1.8e-7 m together, so beyond that band FP64 gives the same answer.
+// Only tests inside the band run in FP64 (this part has few FP64 units).
+struct AbsWithin {
+  double c, r;
+  float cf, rf, tol;
+  bool fast;
+  __device__ __forceinline__ AbsWithin(double c_, double r_) : c(c_), r(r_) {
+    cf = (float)c_;
+    rf = (float)r_;
+    const float m = fabsf(cf) + rf + 1.f;
+    fast = m < 1.0e6f;  // false for NaN too
+    tol = 4.0e-7f * m;
+  }
+  __device__ __forceinline__ bool operator()(int k) const {
+    if (fast) {
+      const float d = fabsf((float)k - cf);
+      if (d <= rf - tol) return true;
+      if (d >= rf + tol) return false;
+    }
+    return fabs((double)k - c) <= r;
+  }
+};
+
 // Inclusive pixel range [lo, hi] of {i : |i - c| <= r}, clipped to [0, n).
 __device__ __forceinline__ void box_bounds(double c, double r, int n, int& lo, int& hi) {
   if (!(r >= 0.0)) {  // NaN or negative range: empty
@@ -244,8 +271,17 @@ __device__ __forceinline__ void box_bounds(double c, double r, int n, int& lo, i
     hi = n - 1;
     return;
   }
-  double a = floor(c - r) - 1.0;
-  double b = ceil(c + r) + 1.0;
+  const AbsWithin in(c, r);
+  // scan start points outside the answer on both sides: FP32 for moderate
+  // coordinates (off by < 0.2 there, so one extra step of margin), FP64 else
+  double a, b;
+  if (in.fast) {
+    a = (double)(floorf(in.cf - in.rf) - 2.f);
+    b = (double)(ceilf(in.cf + in.rf) + 2.f);
+  } else {
+    a = floor(c - r) - 1.0;
+    b = ceil(c + r) + 1.0;
+  }
   if (a < 0.0) a = 0.0;
   if (b > (double)(n - 1)) b = (double)(n - 1);
   if (a > b) {
@@ -254,8 +290,8 @@ __device__ __forceinline__ void box_bounds(double c, double r, int n, int& lo, i
     return;
   }
   int l = (int)a, h = (int)b;
-  while (l <= h && !(fabs((double)l - c) <= r)) ++l;
-  while (h >= l && !(fabs((double)h - c) <= r)) --h;
+  while (l <= h && !in(l)) ++l;
+  while (h >= l && !in(h)) --h;
   lo = l;
   hi = h;
 }
