@@ -135,10 +135,14 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
         rec.h = h;
         rec.inv_h2 = 1.f / (h * h);
         if (g.ks[ks].type <= MG_KERNEL_QUARTIC_SPLINE) {
-          // every table kernel reaches h px; rows outside the cube are never stored
-          const double reach = (double)h * (1.0 + 0x1p-20);
-          const bool lo_in = rec.ilo == 0 || x - (double)(rec.ilo - 1) >= reach;
-          const bool hi_in = rec.ihi == G.nx - 1 || (double)(rec.ihi + 1) - x >= reach;
+          // every table kernel reaches h px; rows outside the cube are never
+          // stored.  Tested in FP32 with a margin well above its rounding
+          // (coordinates below 2^30 px): a flag missed near the edge only
+          // keeps the per-row box test
+          const float xf32 = (float)x;
+          const float reach = h * (1.f + 0x1p-18f) + 1e-6f * (fabsf(xf32) + 1.f);
+          const bool lo_in = rec.ilo == 0 || xf32 - (float)(rec.ilo - 1) >= reach;
+          const bool hi_in = rec.ihi == G.nx - 1 || (float)(rec.ihi + 1) - xf32 >= reach;
           if (lo_in && hi_in) rec.flags |= PREC_ROWS_COVER;
         }
         if (g.spectral_model == MG_SPECTRUM_TABLE) {
@@ -154,7 +158,7 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
           rec.vlo = (float)(v - vh);
           if (g.spectral_model == MG_SPECTRUM_GAUSSIAN) {
             double sg = G.sigma ? (double)G.sigma[p] : (double)G.sigma_const;
-            rec.inv_s = (float)(1.0 / (1.4142135623730951 * sg));
+            rec.inv_s = 1.f / (float)(1.4142135623730951 * sg);  // FP32 division
             // |u| <= 4.5: beyond it each wing holds erfc(4.5) / 2 = 1e-10 of
             // the line's flux
             double half = 4.5 * 1.4142135623730951 * sg;
