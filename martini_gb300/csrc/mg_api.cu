@@ -448,7 +448,7 @@ int mg_plan_batched(const mg_problem* probs, int32_t nprob, void* workspace,
                     size_t workspace_bytes, void* stream, mg_plan_info* info) {
   if (!info) return fail(MG_ERR_INVALID_ARGUMENT, "null info");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Ws w;
+  Ws w{};
   Batch b;
   int rc = run(probs, nprob, workspace, workspace_bytes, s, 0, 0, MG_STAGE_BIN, false, &w, &b);
   if (rc) return rc;
@@ -463,7 +463,7 @@ int mg_plan_batched(const mg_problem* probs, int32_t nprob, void* workspace,
   info->n_tiles = b.g.ntiles;
   size_t spec_bytes = 0;
   if (tc_form(b.g.form) && b.g.spectral_model == MG_SPECTRUM_GAUSSIAN)
-    spec_bytes = align256(sizeof(float) * (size_t)h.spec_bound);
+    spec_bytes = align256(sizeof(unsigned) * (size_t)h.spec_bound);  // packed hi | lo halves
   info->workspace_bytes = layout(b.g, h.n_pairs, h.partial_bound).total + spec_bytes;
   return MG_OK;
 }
