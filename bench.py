@@ -70,7 +70,9 @@ def parse():
     ap.add_argument("--form", default="f16x3", choices=["fp32", "bf16x3", "f16x3"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--n", type=int, default=None, help="override particle count")
-    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0,
+                    help="seconds of host work for the CPU baseline sample (the reference "
+                         "arm takes at most 4x this a step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-gal", type=int, default=200,
                     help="galaxies of the disc population (workload disc_population)")
@@ -658,7 +660,8 @@ def reference_arm(a, rank, world):
     if rank != 0:
         return
     from martini_gb300 import workloads
-    budget = max(2.0, 60.0 / max(1, a.steps + a.warmup))
+    # about a minute of host work in all (at most 4 x --cpu-sample-s a step)
+    budget = min(max(2.0, 60.0 / max(1, a.steps + a.warmup)), 4.0 * a.cpu_sample_s)
     if a.workload == "disc_population":
         # a seeded sample of the population's galaxies; cubes/s from the mean
         # time per cube over the sample
