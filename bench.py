@@ -25,6 +25,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -154,7 +155,9 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{index}.csv")
+        # raw samples (the line carries their summary); MG_CLOCKS_DIR keeps them
+        self.path = os.path.join(os.environ.get("MG_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"martini_gb300_clocks_{index}.csv")
 
     def start(self):
         try:
