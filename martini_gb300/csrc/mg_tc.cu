@@ -532,9 +532,27 @@ __device__ __forceinline__ float half_diff_from_c(float ca, bool pa, float cb, b
 }
 
 // Spectrum store value of channel c for a particle (0 outside its support).
-__device__ __forceinline__ unsigned spec_at(const unsigned* spec, long long soff, const PRec& r,
-                                           bool v, int c) {
-  return (v && c >= r.clo && c <= r.chi) ? __ldg(spec + soff + (c - r.clo)) : 0u;
+// A particle's spectrum-store row: channel clo first, n support channels (0
+// for a particle that contributes nothing, so every lookup gives 0).
+struct SpecRow {
+  const unsigned* row;
+  int clo;
+  unsigned n;
+};
+
+__device__ __forceinline__ SpecRow spec_row(const unsigned* spec, long long soff, const PRec& r,
+                                            bool v) {
+  SpecRow q;
+  q.row = spec + soff;
+  q.clo = r.clo;
+  q.n = (v && r.chi >= r.clo) ? (unsigned)(r.chi - r.clo + 1) : 0u;
+  return q;
+}
+
+// one unsigned compare: c below clo wraps past n
+__device__ __forceinline__ unsigned spec_at(const SpecRow& q, int c) {
+  const unsigned d = (unsigned)(c - q.clo);
+  return d < q.n ? __ldg(q.row + d) : 0u;
 }
 
 // B = S for particles (q, q + 1) over the window channels.  A Gaussian line
@@ -557,6 +575,7 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
     // Gaussian lines read from the spectrum store, already scaled and split
     // (hi | lo << 16 per value); the first 64 window channels were loaded
     // before the weights
+    const SpecRow q0 = spec_row(spec, soff0, r0, v0), q1 = spec_row(spec, soff1, r1, v1);
     for (int base = 0; base < nw; base += 32) {  // warp-uniform
       const int n = base + lane;
       const int c = w0 + n;
@@ -568,8 +587,8 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
         s0 = pf2;
         s1 = pf3;
       } else {
-        s0 = spec_at(spec, soff0, r0, v0, c);
-        s1 = spec_at(spec, soff1, r1, v1, c);
+        s0 = spec_at(q0, c);
+        s1 = spec_at(q1, c);
       }
       if (n < nw) {
         const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
@@ -992,10 +1011,11 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         if (spec) {
           const long long so0 = s_soff[buf][q], so1 = s_soff[buf][q + 1];
           const int wa = it.c0 + w0;
-          pf0 = spec_at(spec, so0, r0, v0, wa + lane);
-          pf1 = spec_at(spec, so1, r1, v1, wa + lane);
-          pf2 = spec_at(spec, so0, r0, v0, wa + 32 + lane);
-          pf3 = spec_at(spec, so1, r1, v1, wa + 32 + lane);
+          const SpecRow q0 = spec_row(spec, so0, r0, v0), q1 = spec_row(spec, so1, r1, v1);
+          pf0 = spec_at(q0, wa + lane);
+          pf1 = spec_at(q1, wa + lane);
+          pf2 = spec_at(q0, wa + 32 + lane);
+          pf3 = spec_at(q1, wa + 32 + lane);
         }
         produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type,
                              smem_u32(s_gtab), q, i0, j0, lane, sw, sa_hi, sa_lo);
