@@ -5,8 +5,6 @@ import ctypes
 import os
 import re
 
-import pytest
-
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "martini_gb300.h")
 LIB = os.path.join(ROOT, "martini_gb300", "libmartini_gb300.so")
