@@ -1,20 +1,30 @@
 """Benchmark of the GPU source insertion (one JSON line on stdout).
 
-A step is one complete ``insert_source_in_cube`` equivalent on the GPU for
-the 1M-particle WendlandC2 disc on a 512 x 512 x 256 cube (thermal Gaussian
-lines): footprint binning, spectra, kernel weights, contraction, cube write
-and FP64 flux sums, from particle arrays resident in HBM.  The metric is
-cubes/s (higher is better); the line also carries particle-channel
-updates/s, the roofline of the dominant kernel (the contraction), the CPU
-baseline (the reference algorithm's per-pixel loop, restated in numpy and
-run on the host cores on a bounded pixel sample) and an end-to-end number
-through the C ABI with host buffers.
+A step is one complete ``insert_source_in_cube`` equivalent on the GPU:
+footprint binning, spectra, kernel weights, contraction, cube write and
+FP64 flux sums, from particle arrays resident in HBM.  The default workload
+is the precision-form configuration: the 4M-particle WendlandC2 disc on a
+1024 x 1024 x 512 cube of 2 km/s channels (thermal Gaussian lines), in the
+chosen tensor-core form (bf16x6, the exact three-piece BF16 split).  The
+metric is cubes/s (higher is better); the line also carries:
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp32|bf16x3]
+* particle-channel updates/s and spectrum evaluations/s;
+* ``fp32``: the plain FP32 CUDA-core form on the same workload;
+* ``errors``: max error / cube peak at 64 sampled pixels and the relative
+  error of the total flux, both against the FP64 CPU oracle;
+* the roofline of the dominant kernel (the contraction);
+* the CPU baseline (the reference algorithm's per-pixel loop, restated in
+  numpy, on a bounded pixel sample and extrapolated: ``timed_fraction``);
+* an end-to-end number through the C ABI with host buffers.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form bf16x6|f16x3|fp32|bf16x3]
+                    [--workload disc4m_1024|disc1m_512|stress16m_2048|disc_population]
     python bench.py --impl reference ...   # the CPU reference arm
 
-Under torchrun (N > 1) every rank inserts its own cube (independent
-replicas, weak scaling); rank 0 prints the line.
+Under torchrun (N > 1) the cube is split into bands of tile rows balanced by
+estimated cost, one per rank with a halo of duplicated particles
+(strong scaling; no collective on the data path); the disc population is
+split into whole cubes per rank, largest first.  Rank 0 prints the line.
 """
 
 from __future__ import annotations
@@ -33,9 +43,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = "disc1m_512"
+WORKLOAD = "disc4m_1024"
 METRIC = "cubes/s & particle-channel updates/s: FP32 vs BF16-split TC, <=1e-5 err vs FP64"
 L2_BYTES = 129 * 1024 * 1024
+# contraction forms (the MG_FORM_* codes)
+FORMS = {"fp32": 0, "bf16x3": 1, "f16x3": 2, "bf16x6": 3}
 # DRAM bytes (read + write) of one launch of the contraction kernel, from
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the full workload;
 # profiles/k_contract_tc_disc1m_512_f16x3.md gives the command and figures
@@ -47,14 +59,15 @@ def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal
     """Kernels one mg_insert(_batched) launches: cube table (one per 16
     cubes), tile init, edges, prep, pair scan (3), difference-array prefix,
     tile scan (3), plan, emit, radix passes x (histogram, scan (3), scatter),
-    segments, item and partial scans (2 x 3), partial check, [spectrum store:
-    row lengths, scan (3), rows], [cube clear for batches], contraction,
-    split-K reduction, flux (3)."""
+    segments, item and partial scans (2 x 3), work-queue keys and their two
+    radix passes (2 x 5), partial check, [spectrum store: row lengths, scan
+    (3), rows], [cube clear for batches], contraction, split-K reduction,
+    flux (3)."""
     if ntiles is None:
         ntiles = ((nx + 7) // 8) * ((ny + 15) // 16)  # 8 x 16-pixel tiles
     bits = max(ntiles - 1, 0).bit_length() + max(nc - 1, 0).bit_length()
     passes = (bits + 7) // 8
-    n = (ngal + 15) // 16 + 1 + 1 + 1 + 3 + 1 + 3 + 1 + 1 + 5 * passes + 1 + 6 + 1
+    n = (ngal + 15) // 16 + 1 + 1 + 1 + 3 + 1 + 3 + 1 + 1 + 5 * passes + 1 + 6 + 1 + 10 + 1
     if form != "fp32" and gaussian:
         n += 1 + 3 + 1
     if ngal > 1:
@@ -68,13 +81,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--form", default="f16x3", choices=["fp32", "bf16x3", "f16x3"])
+    ap.add_argument("--form", default="bf16x6", choices=sorted(FORMS))
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--n", type=int, default=None, help="override particle count")
     ap.add_argument("--cpu-sample-s", type=float, default=15.0,
                     help="seconds of host work for the CPU baseline sample (the reference "
                          "arm takes at most 4x this a step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true",
+                    help="skip timing the plain FP32 form beside the chosen form")
+    ap.add_argument("--no-errors", action="store_true",
+                    help="skip the error fields against the FP64 oracle")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the end-to-end leg (its second buffer set): for profiling")
     ap.add_argument("--n-gal", type=int, default=200,
                     help="galaxies of the disc population (workload disc_population)")
     return ap.parse_args()
@@ -135,9 +154,9 @@ def cpu_baseline(w, budget_s, threads=None):
         batch = min(batch * 2, 4096)
     t_cube = t_spec + t_pix * npix / done
     desc = (f"reference per-pixel loop (numpy restatement) on {done} random pixels of "
-            f"{npix} and spectra of {sub} of {n} particles, scaled to one cube; "
-            f"{threads} threads")
-    return 1.0 / t_cube, threads, desc
+            f"{npix} and spectra of {sub} of {n} particles, extrapolated linearly to one "
+            f"cube; {threads} threads")
+    return 1.0 / t_cube, threads, desc, done / npix
 
 
 # ---------------------------------------------------------------------------
@@ -199,6 +218,157 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def peaks_of():
+    """Roofline denominators: the measured peaks when present, else the
+    fallback figures (and which was used)."""
+    try:
+        pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return (float(pk.get("bf16_tflops", 1900.0)), float(pk.get("hbm_gbs", 6800.0)),
+                "MEASURED_PEAKS.json (bf16_tflops burst, hbm_gbs)")
+    except (OSError, ValueError):
+        return 1900.0, 6800.0, "fallback (1.9 PFLOP/s bf16, 6.8 TB/s)"
+
+
+def roofline(flops, nbytes, t_kernel):
+    """Roofline of one launch: the bound is whichever of the tensor peak and
+    the HBM peak takes longer for the algorithmic work; achieved and frac are
+    in that resource's unit."""
+    peak_tf, peak_gbs, src = peaks_of()
+    t_tensor = flops / (peak_tf * 1e12)
+    t_hbm = nbytes / (peak_gbs * 1e9)
+    if t_tensor >= t_hbm:
+        out = {"bound": "tensor", "achieved": flops / t_kernel / 1e12, "peak": peak_tf,
+               "unit": "TFLOP/s"}
+    else:
+        out = {"bound": "hbm", "achieved": nbytes / t_kernel / 1e9, "peak": peak_gbs,
+               "unit": "GB/s"}
+    out["frac"] = out["achieved"] / out["peak"]
+    out["peak_source"] = src
+    out["algorithmic"] = {"flops": flops, "bytes": nbytes,
+                          "tensor_ms_at_peak": t_tensor * 1e3, "hbm_ms_at_peak": t_hbm * 1e3}
+    return out
+
+
+def band_workload(w, rank, world):
+    """This rank's band of a single-cube workload: contiguous tile rows
+    balanced by estimated pair cost, the particles whose box reaches them
+    (a halo by duplication) with x shifted into the band (shard.shard)."""
+    from martini_gb300 import shard
+    i0, i1, idx, xs = shard.shard(w["x"], w["y"], w["sm_range"], w["nx"], w["ny"], rank, world)
+    sub = dict(w)
+    for k in ("y", "sm_range", "h_eff", "kernel_index", "v", "sigma", "amp", "mHI", "dist"):
+        if isinstance(w.get(k), np.ndarray) and w[k].shape[:1] == (w["n"],):
+            sub[k] = w[k][idx]
+    sub["x"] = xs
+    sub["n"] = int(idx.size)
+    sub["nx"] = int(i1 - i0)
+    sub["band"] = (int(i0), int(i1))
+    if w["groups"]:
+        sub["groups"] = [dict(g, sel=np.flatnonzero(np.isin(idx, g["sel"])))
+                         for g in w["groups"]]
+    return sub
+
+
+def build_insertions(w, form, dev, edges, cube, flux):
+    """One planned insertion per spectral group of the workload; groups after
+    the first add to the cube."""
+    from martini_gb300.engine import DeviceParticles, InsertionEngine
+    groups = w["groups"] or [dict(sel=None, spectral_model=w["spectral_model"])]
+    ins = []
+    for gi, grp in enumerate(groups):
+        s = slice(None) if grp["sel"] is None else grp["sel"]
+        kidx = w["kernel_index"][s] if w["kernel_index"] is not None else None
+        sig = w["sigma"][s] if w["sigma"] is not None else None
+        eng = InsertionEngine(dev)
+        parts = DeviceParticles.from_host(dev, w["x"][s], w["y"][s], w["sm_range"][s],
+                                          w["h_eff"][s], kidx, v=w["v"][s], sigma=sig,
+                                          amp=w["amp"][s])
+        prob = eng.problem(parts, w["kernels"], grp["spectral_model"], w["sigma_const"], w["nx"],
+                           w["ny"], w["nc"], 0, 0, edges, cube, flux, form,
+                           accumulate=gi > 0)
+        info = eng.plan(prob)
+        ins.append(dict(eng=eng, parts=parts, prob=prob, info=info, s=s))
+    return ins
+
+
+def graph_of(ins):
+    """One CUDA graph for a whole step (every group's insertion): the 45-odd
+    launches of an insertion replay as one."""
+    import torch
+    for g in ins:
+        g["eng"].run(g["prob"])
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        for g in ins:
+            g["eng"].run(g["prob"])
+    return graph
+
+
+def timed_steps(fn, k, flush, stream):
+    """K calls of fn, each after an L2 flush, timed with CUDA events on the
+    launching stream (seconds per call)."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(k)]
+    for s0, e0 in ev:
+        flush.zero_()
+        s0.record(stream)
+        fn()
+        e0.record(stream)
+    torch.cuda.synchronize()
+    return [s0.elapsed_time(e0) / 1e3 for s0, e0 in ev]
+
+
+def errors_vs_oracle(w, cube, flux0, max_box_px=6e10):
+    """Max |cube - oracle| / cube peak over 64 sampled pixels (48 with signal,
+    16 uniform; the reference's per-pixel sum in the FP64 oracle) and the
+    relative error of the FP64 flux against the oracle's FP64 total (per
+    particle, in C; skipped when the workload's box pixels exceed
+    max_box_px)."""
+    from martini_gb300 import workloads
+    from oracle import martini_oracle as orc
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(3)
+    lit = np.argwhere(cube.max(axis=2) > 1e-3 * cube.max())
+    pick = lit[rng.choice(len(lit), size=min(48, len(lit)), replace=False)]
+    uni = np.stack([rng.integers(0, cube.shape[0], 16), rng.integers(0, cube.shape[1], 16)], 1)
+    pixels = [tuple(int(v) for v in p) for p in np.concatenate([pick, uni])]
+    kern = orc.adaptive_tuple(w["kernel_name"])
+    groups = w["groups"] or [dict(sel=None, spectral_model=w["spectral_model"])]
+    ref = np.zeros((len(pixels), w["nc"]))
+    total = 0.0
+    box_px = float(workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], w["nx"],
+                                              w["ny"]).sum())
+    do_flux = box_px <= max_box_px
+    for grp in groups:
+        s = np.arange(w["n"]) if grp["sel"] is None else grp["sel"]
+        model = "dirac" if grp["spectral_model"] == FORMS_SPECTRUM_DIRAC else "gaussian"
+        kidx = w["kernel_index"][s] if w["kernel_index"] is not None else None
+        sig = None
+        if model == "gaussian":
+            sig = w["sigma"][s] if w["sigma"] is not None else w["sigma_const"]
+        ref += orc.pixel_spectra(pixels, w["x"][s], w["y"][s], w["sm_range"][s], kern, kidx,
+                                 w["h_eff"][s], model, w["mHI"][s], w["dist"][s], w["v"][s],
+                                 w["edges"], sig)
+        if do_flux:
+            ss = orc.spectrum_sums(model, w["v"][s], sig, w["amp"][s], w["edges"])
+            total += orc.flux_total(w["x"][s], w["y"][s], w["sm_range"][s], kern, kidx,
+                                    w["h_eff"][s].astype(np.float64), ss, w["nx"], w["ny"])
+    got = np.stack([cube[i, j] for i, j in pixels]).astype(np.float64)
+    out = {"max_err_over_peak": float(np.abs(got - ref).max() / np.abs(cube).max()),
+           "pixels_sampled": len(pixels),
+           "flux_rel_err": float(abs(flux0 - total) / total) if do_flux else None,
+           "oracle": "FP64 CPU oracle: per-pixel sums at the sampled pixels; total flux as "
+                     "sum_p (sum_box W_p)(sum_c S_p) over every particle" +
+                     ("" if do_flux else " (skipped: too many box pixels for the host)"),
+           "oracle_s": round(time.perf_counter() - t0, 2)}
+    return out
+
+
+FORMS_SPECTRUM_DIRAC = 1  # MG_SPECTRUM_DIRAC
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
@@ -209,7 +379,6 @@ def main():
     import torch.distributed as dist
     from martini_gb300 import _native as N
     from martini_gb300 import workloads
-    from martini_gb300.engine import DeviceParticles, InsertionEngine
 
     if world > 1:
         torch.cuda.set_device(local)
@@ -221,39 +390,18 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return
-    w = workloads.build(a.workload, n=a.n)
-    form = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}[a.form]
+    w_full = workloads.build(a.workload, n=a.n)
+    # one cube per step: with N ranks each inserts its own band of it
+    w = band_workload(w_full, rank, world) if world > 1 else w_full
+    form = FORMS[a.form]
     edges = torch.from_numpy(np.ascontiguousarray(w["edges"])).to(dev)
     nx, ny, nc = w["nx"], w["ny"], w["nc"]
     cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=dev)
     flux = torch.empty(nc + 1, dtype=torch.float64, device=dev)
-    # one insertion per spectral group; later groups add to the cube
-    groups = w["groups"] or [dict(sel=None, spectral_model=w["spectral_model"])]
-    ins = []
-    for gi, grp in enumerate(groups):
-        s = slice(None) if grp["sel"] is None else grp["sel"]
-        kidx = w["kernel_index"][s] if w["kernel_index"] is not None else None
-        sig = w["sigma"][s] if w["sigma"] is not None else None
-        eng = InsertionEngine(dev)
-        parts = DeviceParticles.from_host(dev, w["x"][s], w["y"][s], w["sm_range"][s],
-                                          w["h_eff"][s], kidx, v=w["v"][s], sigma=sig,
-                                          amp=w["amp"][s])
-        prob = eng.problem(parts, w["kernels"], grp["spectral_model"], w["sigma_const"], nx, ny,
-                           nc, 0, 0, edges, cube, flux, form, accumulate=gi > 0)
-        info = eng.plan(prob)
-        ins.append(dict(eng=eng, parts=parts, prob=prob, info=info, s=s))
+    ins = build_insertions(w, form, dev, edges, cube, flux)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
-
-    # one CUDA graph for the whole step (every group's insertion): the 45-odd
-    # launches of an insertion replay as one
-    for g in ins:
-        g["eng"].run(g["prob"])
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph):
-        for g in ins:
-            g["eng"].run(g["prob"])
+    graph = graph_of(ins)
 
     def step():
         graph.replay()
@@ -274,36 +422,124 @@ def main():
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(a.steps)]
-    for k in range(a.steps):
-        flush.zero_()
-        ev[k][0].record(stream)
-        step()
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
+    t_step = timed_steps(step, a.steps, flush, stream)
     if world > 1:
         dist.barrier()
     clk = clocks.stop()
-    t_steps = sum(s.elapsed_time(e) for s, e in ev) / 1e3  # s
+    t_steps = float(np.sum(t_step))
     for g in ins:
         g["eng"].check()
+    cube_host = cube.cpu().numpy() if rank == 0 else None
+    flux0 = float(flux[0].item())
 
     # --- dominant kernel: the contraction stage alone ------------------------
     for g in ins:
         g["eng"].run_stages(g["prob"], N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
-    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(3)]
-    for s0, e0 in cev:
+    t_contract = float(np.mean(timed_steps(
+        lambda: [g["eng"].run_stages(g["prob"], N.MG_STAGE_CONTRACT) for g in ins], 3, flush,
+        stream)))
+
+    # --- the plain FP32 form on the same workload -----------------------------
+    fp32 = None
+    if form != FORMS["fp32"] and not a.no_fp32 and world == 1:
+        cube32 = torch.empty_like(cube)
+        flux32 = torch.empty_like(flux)
+        ins32 = build_insertions(w, FORMS["fp32"], dev, edges, cube32, flux32)
+        g32 = graph_of(ins32)
         flush.zero_()
-        s0.record(stream)
-        for g in ins:
-            g["eng"].run_stages(g["prob"], N.MG_STAGE_CONTRACT)
-        e0.record(stream)
-    torch.cuda.synchronize()
-    t_contract = float(np.mean([s0.elapsed_time(e0) for s0, e0 in cev])) / 1e3
+        g32.replay()
+        t32 = timed_steps(g32.replay, max(3, min(a.steps, 5)), flush, stream)
+        for g in ins32:
+            g["eng"].check()
+        fp32 = {"value": len(t32) / float(np.sum(t32)), "unit": "cubes/s",
+                "ms_per_step": float(np.mean(t32)) * 1e3}
+        del ins32, g32, cube32, flux32
+        torch.cuda.empty_cache()
 
     # --- end to end through the C ABI with host buffers -------------------------
+    t_e2e, h2d, d2h = (float("nan"), 0, 0) if a.no_e2e else e2e_time(a, w, ins, cube, flux,
+                                                                      form, edges, dev, stream)
+
+    # --- aggregate over ranks ---------------------------------------------------
+    if world > 1:
+        tt = torch.tensor([t_steps, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_steps, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # algorithmic work: box-footprint pixels x channels (the reference's
+    # per-pixel mask selects exactly these pairs), of the whole cube
+    F = workloads.footprint_pixels(w_full["x"], w_full["y"], w_full["sm_range"], w_full["nx"],
+                                   w_full["ny"])
+    updates = float(F.sum()) * w_full["nc"]
+    cubes_per_s = a.steps / t_steps
+    # roofline of this rank's contraction launch: its own band's work
+    Fr = workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], nx, ny)
+    flops_r = 2.0 * float(Fr.sum()) * nc
+    bytes_r = float(nx) * ny * nc * 4 + 72.0 * w["n"]
+    rl = roofline(flops_r, bytes_r, t_contract)
+    rl["kernel"] = (("k_contract_tc" if a.form != "fp32" else "k_contract_fp32") +
+                    " (stage timed: cube clear, contraction, split-K reduction)")
+    rl["contract_ms"] = t_contract * 1e3
+    # measured on the full workload only: no figure for a reduced particle count
+    rl["traffic"] = (TRAFFIC_BYTES.get((a.workload, a.form))
+                     if a.n is None and world == 1 else None)
+    err = errors_vs_oracle(w, cube_host, flux0) if not a.no_errors else None
+    line = {
+        "metric": METRIC,
+        "value": cubes_per_s,
+        "unit": "cubes/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": t_steps / a.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "strong" if world > 1 else "weak",
+        "vs_baseline": None,
+        "dtype": a.form,
+        "data": "synthetic (seeded exponential disc, no dataset)",
+        "config": {"workload": a.workload, "particles": w_full["n"], "particles_generated":
+                   w_full["n_input"], "cube": [w_full["nx"], w_full["ny"], w_full["nc"]],
+                   "kernel": w_full["kernel_name"], "spectrum": w_full["spectral_kind"],
+                   "form": a.form, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"bands{world}" if world > 1 else "single",
+                   "pairs": int(sum(g["info"].n_pairs for g in ins)), "groups": len(ins)},
+        "particle_channel_updates_per_s": updates * a.steps / t_steps,
+        "spectrum_evaluations_per_s": float(w_full["n"]) * w_full["nc"] * a.steps / t_steps,
+        "errors": err,
+        "fp32": fp32,
+        "roofline": rl,
+        "e2e": {"value": 1.0 / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": a.steps * sum(launches_per_step(
+            a.form, g["prob"].spectral_model == N.MG_SPECTRUM_GAUSSIAN, nx, ny, nc) for g in ins),
+        "step_ms": [round(t * 1e3, 3) for t in t_step],
+        "clocks": clk,
+    }
+    if world > 1:
+        line["config"]["band_rows_rank0"] = w["band"]
+    if not a.no_cpu_baseline:
+        v, cores, desc, frac = cpu_baseline(w_full, a.cpu_sample_s)
+        line["cpu_baseline"] = {"value": v, "unit": "cubes/s", "cores": cores, "kind": "port",
+                                "sample": desc, "extrapolated": True, "timed_fraction": frac}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def e2e_time(a, w, ins, cube, flux, form, edges, dev, stream):
+    """Seconds per cube end to end through the C ABI: every step copies its
+    particles from pinned host memory and reads the cube and flux back.  Two
+    buffer sets (device particles, cube, flux; pinned host results) so that
+    the copies of one step overlap the insertion of the next: inputs go up
+    and results come back on copy streams, insertions run in order on the
+    compute stream (one workspace per engine).  Returns (s, h2d, d2h bytes)."""
+    import dataclasses
+    import torch
+    nx, ny, nc = w["nx"], w["ny"], w["nc"]
     for g in ins:
         s = g["s"]
         host = {k: torch.from_numpy(np.ascontiguousarray(w[k][s], dtype=dt)).pin_memory()
@@ -316,11 +552,6 @@ def main():
             host["sigma"] = torch.from_numpy(w["sigma"][s].astype(np.float32)).pin_memory()
         g["host"] = host
         g["dev"] = {k: getattr(g["parts"], k) for k in host}
-    # two buffer sets (device particles, cube, flux; pinned host results) so
-    # that the copies of one step overlap the insertion of the next: inputs
-    # go up and results come back on a copy stream, insertions run in order
-    # on the compute stream (one workspace per engine)
-    import dataclasses
     sets = [dict(cube=cube, flux=flux, probs=[g["prob"] for g in ins],
                  dev=[g["dev"] for g in ins])]
     cube1, flux1 = torch.empty_like(cube), torch.empty_like(flux)
@@ -381,74 +612,9 @@ def main():
     stream.wait_event(down_ev[ke - 2])
     e1.record(stream)
     torch.cuda.synchronize()
-    t_e2e = e0.elapsed_time(e1) / 1e3 / ke
-
-    # --- aggregate over ranks ---------------------------------------------------
-    if world > 1:
-        tt = torch.tensor([t_steps, t_e2e], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_steps, t_e2e = float(tt[0]), float(tt[1])
-    if rank != 0:
-        if world > 1:
-            dist.destroy_process_group()
-        return
-
-    # algorithmic work: box-footprint pixels x channels (the reference's
-    # per-pixel mask selects exactly these pairs)
-    F = workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], nx, ny)
-    updates = float(F.sum()) * nc
-    flops = 2.0 * updates
-    cubes_per_s = world * a.steps / t_steps
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak_tf = peaks.get("bf16_tflops", 1900.0)
-    achieved_tf = flops / t_contract / 1e12
-    # measured on the full workload only: no figure for a reduced particle count
-    traffic = TRAFFIC_BYTES.get((a.workload, a.form)) if a.n is None else None
-    line = {
-        "metric": METRIC,
-        "value": cubes_per_s,
-        "unit": "cubes/s",
-        "n_gpus": world,
-        "steps": a.steps,
-        "warmup": a.warmup,
-        "ms_per_step": t_steps / a.steps * 1e3,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": a.form,
-        "data": "synthetic (seeded exponential disc, no dataset)",
-        "config": {"workload": a.workload, "particles": w["n"], "particles_generated":
-                   w["n_input"], "cube": [nx, ny, nc], "kernel": w["kernel_name"],
-                   "spectrum": w["spectral_kind"], "form": a.form,
-                   "l2": "flushed between steps (256 MiB write)", "parallelism":
-                   f"replicas{world}", "pairs": int(sum(g["info"].n_pairs for g in ins)),
-                   "groups": len(ins)},
-        "particle_channel_updates_per_s": world * updates * a.steps / t_steps,
-        "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf,
-                     "unit": "TFLOP/s", "frac": achieved_tf / peak_tf, "traffic": traffic,
-                     "kernel": ("k_contract_tc" if a.form != "fp32" else "k_contract_fp32")
-                     + " (stage timed: cube clear, contraction, split-K reduction)",
-                     "contract_ms": t_contract * 1e3,
-                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks
-                     else "fallback 1.9 PFLOP/s"},
-        "e2e": {"value": world / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": a.steps * sum(launches_per_step(
-            a.form, g["prob"].spectral_model == N.MG_SPECTRUM_GAUSSIAN, nx, ny, nc) for g in ins),
-        "step_ms": [round(s.elapsed_time(e), 3) for s, e in ev],
-        "clocks": clk,
-    }
-    if not a.no_cpu_baseline:
-        v, cores, desc = cpu_baseline(w, a.cpu_sample_s)
-        line["cpu_baseline"] = {"value": v, "unit": "cubes/s", "cores": cores, "kind": "port",
-                                "sample": desc}
-    print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    for g in ins:
+        g["eng"].check()
+    return e0.elapsed_time(e1) / 1e3 / ke, h2d, d2h
 
 
 def run_population(a, rank, world, local, dev):
@@ -460,8 +626,20 @@ def run_population(a, rank, world, local, dev):
     from martini_gb300 import workloads
     from martini_gb300.engine import BatchInsertion, DeviceParticles, InsertionEngine
 
-    form = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}[a.form]
-    gals = workloads.build_population(a.n_gal, workers=0)
+    form = FORMS[a.form]
+    gals_all = workloads.build_population(a.n_gal, workers=0)
+    gals = gals_all
+    imbalance = None
+    if world > 1:
+        # whole cubes per rank, largest estimated cost first to the least
+        # loaded rank (shard.assign_galaxies); no exchange step
+        from martini_gb300 import shard
+        cost = [float(workloads.footprint_pixels(g["x"], g["y"], g["sm_range"], g["nx"],
+                                                 g["ny"]).sum()) * g["nc"] for g in gals_all]
+        parts_of = shard.assign_galaxies(cost, world)
+        loads = [sum(cost[k] for k in ks) for ks in parts_of]
+        imbalance = max(loads) / (sum(loads) / world) if sum(loads) > 0 else 1.0
+        gals = [gals_all[k] for k in parts_of[rank]]
     eng = InsertionEngine(dev)
     items, probs = [], []
     for w in gals:
@@ -615,40 +793,39 @@ def run_population(a, rank, world, local, dev):
         tb, tl, t_e2e = (float(v) for v in tt)
     if rank != 0:
         return
-    ng = len(gals)
+    ng = len(gals_all)
     updates = float(sum(workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], w["nx"],
-                                                   w["ny"]).sum() * w["nc"] for w in gals))
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak_tf = peaks.get("bf16_tflops", 1900.0)
-    achieved = 2.0 * updates / t_contract / 1e12
+                                                   w["ny"]).sum() * w["nc"] for w in gals_all))
+    updates_r = float(sum(workloads.footprint_pixels(w["x"], w["y"], w["sm_range"], w["nx"],
+                                                     w["ny"]).sum() * w["nc"] for w in gals))
+    bytes_r = float(sum(w["nx"] * w["ny"] * w["nc"] * 4 + 72 * w["n"] for w in gals))
+    rl = roofline(2.0 * updates_r, bytes_r, t_contract)
+    rl.update({"traffic": None, "contract_ms": t_contract * 1e3,
+               "kernel": "k_contract_tc (stage timed: cube clear, contraction, split-K "
+                         "reduction, all cubes)"})
     ntiles = sum(((w["nx"] + 7) // 8) * ((w["ny"] + 15) // 16) for w in gals)
     line = {
-        "metric": METRIC, "value": world * ng * a.steps / tb, "unit": "cubes/s", "n_gpus": world,
+        "metric": METRIC, "value": ng * a.steps / tb, "unit": "cubes/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": tb / a.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": a.form,
+        "higher_is_better": True, "scaling": "strong" if world > 1 else "weak",
+        "vs_baseline": None, "dtype": a.form,
         "data": "synthetic (seeded disc population, no dataset)",
         "config": {"workload": "disc_population", "galaxies": ng,
                    "particles": int(sum(w["n"] for w in gals)),
                    "cubes": "32^2x64 | 64^2x128 | 128^2x128 | 256^2x256 at 4 km/s",
                    "kernel": "WendlandC2Kernel", "spectrum": "thermal", "form": a.form,
                    "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": f"replicas{world}", "pairs": int(info.n_pairs),
-                   "form_batched": True},
-        "looped": {"value": world * ng * a.steps / tl, "unit": "cubes/s",
+                   "parallelism": f"lpt{world}" if world > 1 else "single",
+                   "pairs_rank0": int(info.n_pairs), "form_batched": True,
+                   "lpt_imbalance": imbalance},
+        "looped": {"value": ng * a.steps / tl, "unit": "cubes/s",
                    "ms_per_step": tl / a.steps * 1e3,
                    "note": "same cubes, one mg_insert per cube"},
-        "particle_channel_updates_per_s": world * updates * a.steps / tb,
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf,
-                     "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
-                     "kernel": "k_contract_tc (stage timed: cube clear, contraction, split-K "
-                               "reduction, all cubes)", "contract_ms": t_contract * 1e3,
-                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks
-                     else "fallback 1.9 PFLOP/s"},
-        "e2e": {"value": world * ng / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
+        "particle_channel_updates_per_s": updates * a.steps / tb,
+        "spectrum_evaluations_per_s": float(sum(w["n"] * w["nc"] for w in gals_all)) * a.steps
+                                      / tb,
+        "roofline": rl,
+        "e2e": {"value": ng / t_e2e, "unit": "cubes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": a.steps * launches_per_step(a.form, True, 0, 0,
                                                     max(w["nc"] for w in gals), ng, ntiles),
@@ -675,13 +852,15 @@ def reference_arm(a, rank, world):
                  kernel_name="WendlandC2Kernel", spectral_kind="thermal")
 
         def one(b):
-            tsum = 0.0
+            tsum, fr = 0.0, []
             for g in sample:
-                v, cores, _ = cpu_baseline(g, b / len(sample))
+                v, cores, _, f = cpu_baseline(g, b / len(sample))
                 tsum += 1.0 / v
-            return len(sample) / tsum, cores, (f"reference per-pixel loop (numpy restatement) on "
-                                               f"{len(sample)} sampled galaxies of {len(gals)}, "
-                                               f"each on a pixel sample, scaled to whole cubes")
+                fr.append(f)
+            return (len(sample) / tsum, cores,
+                    f"reference per-pixel loop (numpy restatement) on {len(sample)} sampled "
+                    f"galaxies of {len(gals)}, each on a pixel sample, extrapolated linearly to "
+                    f"whole cubes", float(np.mean(fr)) * len(sample) / len(gals))
     else:
         w = workloads.build(a.workload, n=a.n)
 
@@ -689,11 +868,12 @@ def reference_arm(a, rank, world):
             return cpu_baseline(w, b)
     for _ in range(a.warmup):
         one(budget / 4)
-    vals = []
+    vals, fracs = [], []
     t0 = time.perf_counter()
     for _ in range(a.steps):
-        v, cores, desc = one(budget)
+        v, cores, desc, frac = one(budget)
         vals.append(v)
+        fracs.append(frac)
     wall = time.perf_counter() - t0
     value = float(np.mean(vals))
     line = {
@@ -705,7 +885,8 @@ def reference_arm(a, rank, world):
         "config": {"workload": a.workload, "particles": w["n"], "cube": [w["nx"], w["ny"], w["nc"]],
                    "kernel": w["kernel_name"], "spectrum": w["spectral_kind"]},
         "cpu_baseline": {"value": value, "unit": "cubes/s", "cores": cores, "kind": "port",
-                         "sample": desc},
+                         "sample": desc, "extrapolated": True,
+                         "timed_fraction": float(np.mean(fracs))},
         "e2e": {"value": value, "unit": "cubes/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "wall_s": wall,

@@ -17,7 +17,7 @@
  * ``_BaseSpectrum.init_spectra`` (martini/spectral_models.py:63-200,
  * :386-425, :544-570).  The reference is pure Python and has no FFI; these
  * entry points are what a ctypes/cffi binding of ``_insert_source_in_cube``
- * calls (see INTEGRATION.md).
+ * calls.
  *
  * Conventions
  *   - All array pointers are DEVICE pointers owned by the caller.
@@ -61,8 +61,13 @@ extern "C" {
 
 /* contraction forms */
 #define MG_FORM_FP32 0            /* FP32 CUDA-core contraction */
-#define MG_FORM_BF16X3 1          /* BF16 hi+lo split, three tcgen05 products */
+#define MG_FORM_BF16X3 1          /* BF16 hi+lo split, three tcgen05 products (~16 bits per
+                                     operand: about 1e-5 relative per term, below the
+                                     1e-5-of-peak / 1e-6-of-flux bar only on average) */
 #define MG_FORM_F16X3 2           /* FP16 hi+lo split (power-of-two scaled), three tcgen05 products */
+#define MG_FORM_BF16X6 3          /* BF16 hi+mid+lo split (exact for FP32 operands: 24 bits in
+                                     three 8-bit pieces), six tcgen05 products (every cross term
+                                     down to 2^-16 relative); the chosen tensor-core form */
 
 #define MG_MAX_KERNELS 4
 
@@ -322,11 +327,15 @@ int mg_flux(const float* cube, int32_t nx, int32_t ny, int32_t nc, int32_t padx,
  * it exists for callers that cannot allocate GPU memory (code inside a
  * framework or memory pool that owns every device allocation, or paths where
  * an allocation is not allowed).  The scratch is a file-scope device array of
- * MG_NOALLOC_SCRATCH_BYTES; problems whose binning needs more are rejected
- * with MG_ERR_WORKSPACE and a message.  The first call on a device looks up
- * the array's device address (make it before any stream capture).  Calls
- * share the array: calls that overlap on the GPU race.  Synchronises the
- * stream (it checks the status word); allocates nothing.
+ * MG_NOALLOC_SCRATCH_BYTES; a problem whose fixed workspace part alone is
+ * larger is rejected before any GPU work, and one whose binning turns out to
+ * need more pairs or split-K tiles than the array holds returns
+ * MG_ERR_WORKSPACE with a message naming the built-in scratch.  Every call
+ * looks up the array's device address on the current device (nothing is
+ * cached, so a device reset cannot leave a stale address).  Calls share the
+ * array: calls that overlap on the GPU race.  Every call synchronises the
+ * stream (it reads the status word back), so no call can be captured in a
+ * CUDA graph.  Allocates nothing.
  */
 int mg_insert_noalloc(const mg_problem* p, void* stream);
 

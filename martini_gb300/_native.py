@@ -35,6 +35,7 @@ MG_SPECTRUM_TABLE = 2
 MG_FORM_FP32 = 0
 MG_FORM_BF16X3 = 1
 MG_FORM_F16X3 = 2
+MG_FORM_BF16X6 = 3
 
 MG_MAX_KERNELS = 4
 

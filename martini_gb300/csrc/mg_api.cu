@@ -28,12 +28,17 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+bool known_form(int form) {
+  return form == MG_FORM_FP32 || form == MG_FORM_BF16X3 || form == MG_FORM_F16X3 ||
+         form == MG_FORM_BF16X6;
+}
+
 // Segment shape of a contraction form: channel blocks per tile and their
 // width.  Tensor-core forms: the band (rounded to 16) in one block up to 256
 // channels, else blocks of 256 (a block and its master accumulator fill the
 // 512 TMEM columns).
 void seg_shape(int form, int nc, int* ncb, int* width) {
-  if (form == MG_FORM_BF16X3 || form == MG_FORM_F16X3) {
+  if (form == MG_FORM_BF16X3 || form == MG_FORM_F16X3 || form == MG_FORM_BF16X6) {
     if (nc <= 256) {
       *ncb = 1;
       *width = (nc + 15) / 16 * 16;
@@ -57,7 +62,8 @@ struct Layout {
   size_t hdr, gal, gst, gp0, gt0, gs0, ge0, gr0, rec, npairs, pair_off, tile_count, tile_diff,
       tile_off, ehi, elo, inv_w, keys, list, keys_tmp, list_tmp, rs_hist,
       rs_off, scan_sums, seg_lo, seg_hi, seg_items, seg_part, item_off, part_off, partial,
-      flux_part, total;
+      flux_part, item_order, item_key, item_key_tmp, item_order_tmp, total;
+  long long cap_items;
 };
 
 Layout layout(const Geo& g, long long cap_pairs, long long cap_partial) {
@@ -107,6 +113,12 @@ Layout layout(const Geo& g, long long cap_pairs, long long cap_partial) {
   L.item_off = take(sizeof(long long) * (size_t)g.nseg);
   L.part_off = take(sizeof(long long) * (size_t)g.nseg);
   L.flux_part = take(sizeof(double) * (size_t)g.nfpart);
+  L.cap_items = items_bound(g.nseg, cap_pairs > 0 ? cap_pairs : 0);
+  const size_t ci = (size_t)(L.cap_items > 0 ? L.cap_items : 1);
+  L.item_order = take(sizeof(int) * ci);
+  L.item_key = take(sizeof(unsigned) * ci);
+  L.item_key_tmp = take(sizeof(unsigned) * ci);
+  L.item_order_tmp = take(sizeof(int) * ci);
   L.partial = take(sizeof(float) * (size_t)TILE_PX * g.max_width *
                    (size_t)(cap_partial > 0 ? cap_partial : 0));
   L.total = o;
@@ -150,6 +162,11 @@ Ws make_ws(void* base, const Layout& L) {
   w.flux_part = reinterpret_cast<double*>(b + L.flux_part);
   w.spec = nullptr;
   w.cap_spec = 0;
+  w.item_order = reinterpret_cast<int*>(b + L.item_order);
+  w.item_key = reinterpret_cast<unsigned*>(b + L.item_key);
+  w.item_key_tmp = reinterpret_cast<unsigned*>(b + L.item_key_tmp);
+  w.item_order_tmp = reinterpret_cast<int*>(b + L.item_order_tmp);
+  w.cap_items = L.cap_items;
   return w;
 }
 
@@ -184,7 +201,7 @@ int check_problem(const mg_problem* p) {
   }
   if (p->n > 0 && (!p->x || !p->y || !p->sm_range || !p->h_eff))
     return fail(MG_ERR_INVALID_ARGUMENT, "x, y, sm_range and h_eff are required");
-  if (p->form != MG_FORM_FP32 && p->form != MG_FORM_BF16X3 && p->form != MG_FORM_F16X3)
+  if (!known_form(p->form))
     return fail(MG_ERR_INVALID_ARGUMENT, "unknown contraction form");
   for (int k = 0; k < p->n_kernels; ++k) {
     const int t = p->kernels[k].type;
@@ -219,7 +236,7 @@ int make_batch(const mg_problem* probs, int nprob, Batch* b, bool shape_only = f
       rc = fail(MG_ERR_INVALID_ARGUMENT, "invalid problem dimensions");
     } else if (p.padx < 0 || p.pady < 0 || 2 * p.padx >= p.nx || 2 * p.pady >= p.ny) {
       rc = fail(MG_ERR_INVALID_ARGUMENT, "invalid pad");
-    } else if (p.form != MG_FORM_FP32 && p.form != MG_FORM_BF16X3 && p.form != MG_FORM_F16X3) {
+    } else if (!known_form(p.form)) {
       rc = fail(MG_ERR_INVALID_ARGUMENT, "unknown contraction form");
     }
     if (rc) return rc;
@@ -327,7 +344,9 @@ int num_sms() {
   return sms[dev];
 }
 
-bool tc_form(int form) { return form == MG_FORM_BF16X3 || form == MG_FORM_F16X3; }
+bool tc_form(int form) {
+  return form == MG_FORM_BF16X3 || form == MG_FORM_F16X3 || form == MG_FORM_BF16X6;
+}
 
 int workspace_view(const Geo& g, void* ws, size_t bytes, long long cap_pairs,
                    long long cap_partial, Ws* w) {
@@ -426,7 +445,8 @@ int run(const mg_problem* probs, int nprob, void* ws, size_t bytes, cudaStream_t
       if (rc == MG_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tensor-core kernel set-up");
       if (rc) return fail(rc, "tensor-core form does not support this cube (band too wide)");
     } else {
-      launch_contract_fp32(g, w, num_sms(), s);
+      rc = launch_contract_fp32(g, w, num_sms(), s);
+      if (rc) return cuda_fail(cudaGetLastError(), "FP32 contraction set-up");
     }
   }
   if (stages & MG_STAGE_FLUX) {
@@ -463,7 +483,9 @@ int mg_plan_batched(const mg_problem* probs, int32_t nprob, void* workspace,
   info->n_tiles = b.g.ntiles;
   size_t spec_bytes = 0;
   if (tc_form(b.g.form) && b.g.spectral_model == MG_SPECTRUM_GAUSSIAN)
-    spec_bytes = align256(sizeof(unsigned) * (size_t)h.spec_bound);  // packed hi | lo halves
+    // one 32-bit word per support channel: packed hi | lo halves, or the FP32
+    // value the three-piece BF16 split is taken from
+    spec_bytes = align256(sizeof(unsigned) * (size_t)h.spec_bound);
   info->workspace_bytes = layout(b.g, h.n_pairs, h.partial_bound).total + spec_bytes;
   return MG_OK;
 }

@@ -486,6 +486,35 @@ __global__ void k_segments(Geo g, Ws w) {
   }
 }
 
+// Work-queue keys: one thread per segment writes the keys of its items
+// (item k of a segment holds min(kch, cnt - k kch) particles).  Estimated
+// cost = particles x (2 TILE_PX + width): the kernel weights at the tile's
+// pixels and the spectra and products over the segment's channel block.
+// Key = 65535 - cost scaled to 16 bits, so that the stable ascending radix
+// sort puts the largest items first and keeps segment order among equal
+// ones: the persistent contraction then ends on the small items instead of
+// leaving one large item to a single SM at the end.
+__global__ void k_item_keys(Geo g, Ws w) {
+  if (w.hdr->status & (ST_PAIRS | ST_EDGES)) return;
+  const int kch = w.hdr->kch;
+  const double cmax = (double)kch * (2.0 * TILE_PX + (double)g.max_width);
+  for (int sg = blockIdx.x * blockDim.x + threadIdx.x; sg < g.nseg; sg += gridDim.x * blockDim.x) {
+    const int n_it = w.seg_items[sg];
+    if (n_it == 0) continue;
+    const long long base = w.item_off[sg];
+    const long long cnt = w.seg_hi[sg] - w.seg_lo[sg];
+    const int width = w.gal[find_gal(w.gs0, g.ngal, sg)].width;
+    for (int k = 0; k < n_it && base + k < w.cap_items; ++k) {
+      const long long left = cnt - (long long)k * kch;
+      const double lc = (double)(left < kch ? left : kch);
+      double q = lc * (2.0 * TILE_PX + (double)width) / cmax * 65535.0 + 0.5;
+      if (q > 65535.0) q = 65535.0;
+      w.item_key[base + k] = 65535u - (unsigned)q;
+      w.item_order[base + k] = (int)(base + k);
+    }
+  }
+}
+
 __global__ void k_check_partials(Ws w) {
   WsHeader* h = w.hdr;
   if (h->n_partial_items > h->cap_partial_items) h->status |= ST_PARTIALS;
@@ -552,6 +581,11 @@ void launch_sort_segments(const Geo& g, const Ws& w, long long cap_pairs, int nu
   k_segments<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, w);
   launch_scan(w.seg_items, g.nseg, w.item_off, w.scan_sums, &w.hdr->n_items, s);
   launch_scan(w.seg_part, g.nseg, w.part_off, w.scan_sums, &w.hdr->n_partial_items, s);
+  // the work queue: items by estimated cost, largest first (16-bit keys: two
+  // radix passes, the result back in item_key / item_order)
+  k_item_keys<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, w);
+  launch_radix_sort(w.item_key, w.item_order, w.item_key_tmp, w.item_order_tmp, &w.hdr->n_items,
+                    w.cap_items, 16, w.rs_hist, w.rs_off, w.scan_sums, num_sms, s);
   k_check_partials<<<1, 1, 0, s>>>(w);
 }
 

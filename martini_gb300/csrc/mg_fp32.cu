@@ -11,6 +11,7 @@ namespace mg {
 
 constexpr int F32_THREADS = 256;
 constexpr int F32_KC = 32;  // particles per shared-memory chunk
+constexpr int F32_MASTER_BYTES = 32 * F32_THREADS * 4;  // master accumulators (dynamic)
 
 // Segment of work item `item`: the largest sg with item_off[sg] <= item
 // (segments without items share their successor's offset).
@@ -55,6 +56,15 @@ __global__ void __launch_bounds__(F32_THREADS, 2)
 k_contract_fp32(Geo g, Ws w) {
   __shared__ __align__(16) float Ws_[F32_KC][TILE_PX];
   __shared__ __align__(16) float Ss_[F32_KC][CBLK];
+  // Master accumulator: each F32_KC-particle chunk is summed from zero in
+  // registers and added here (round to nearest).  One running FP32 sum over
+  // an item's particles (up to ~10^6 on a dense tile) drops every product
+  // below half an ulp of the sum, a loss that only grows with the count; a
+  // chunk sum of 32 products meets the master far less often.  Laid out
+  // [value][thread] in dynamic shared memory (F32_MASTER_BYTES): each
+  // thread's slots are conflict-free.
+  extern __shared__ float Ms_dyn[];
+  float(*Ms_)[F32_THREADS] = reinterpret_cast<float(*)[F32_THREADS]>(Ms_dyn);
   __shared__ PRec recs[F32_KC];
   __shared__ int s_pid[F32_KC];
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
@@ -75,7 +85,8 @@ k_contract_fp32(Geo g, Ws w) {
     const long long item = s_item;
     __syncthreads();
     if (item >= n_items) break;
-    const ItemInfo it = decode_item(g, w, item, kch);
+    // the queue runs over the items in cost order, largest first
+    const ItemInfo it = decode_item(g, w, (long long)w.item_order[item], kch);
     const Gal& G = w.gal[it.gal];
     const int dec = w.gst[it.gal].dec;
     const int nc = G.nc;
@@ -89,6 +100,8 @@ k_contract_fp32(Geo g, Ws w) {
     for (int a = 0; a < 8; ++a)
 #pragma unroll
       for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+#pragma unroll
+    for (int v = 0; v < 32; ++v) Ms_[v][tid] = 0.f;
 
     for (int k0 = 0; k0 < it.lcount; k0 += F32_KC) {
       const int kn = min(F32_KC, it.lcount - k0);
@@ -146,8 +159,20 @@ k_contract_fp32(Geo g, Ws w) {
           acc[a][3] = fmaf(wv[a], s.w, acc[a][3]);
         }
       }
+      // chunk sum into the master, registers back to zero
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          Ms_[a * 4 + b][tid] += acc[a][b];
+          acc[a][b] = 0.f;
+        }
       __syncthreads();
     }
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = Ms_[a * 4 + b][tid];
 
     // epilogue: direct cube write (single K chunk) or split-K partial
     if (it.nk == 1) {
@@ -329,9 +354,22 @@ void launch_flux(const float* cube, int nx, int ny, int nc, int padx, int pady, 
   k_flux_final<<<1, 1024, 0, s>>>(part, nch, nc, flux);
 }
 
-void launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
-  k_contract_fp32<<<num_sms * 2, F32_THREADS, 0, s>>>(g, w);
+int launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
+  // the dynamic shared-memory attribute is per device: set once on each
+  // (host-side, before a graph capture by the first insertion on a device)
+  constexpr int kMaxDev = 64;
+  static bool attr_set[kMaxDev] = {false};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return MG_ERR_CUDA;
+  if (!attr_set[dev]) {
+    if (cudaFuncSetAttribute(k_contract_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             F32_MASTER_BYTES) != cudaSuccess)
+      return MG_ERR_CUDA;
+    attr_set[dev] = true;
+  }
+  k_contract_fp32<<<num_sms * 2, F32_THREADS, F32_MASTER_BYTES, s>>>(g, w);
   launch_reduce_partials(g, w, num_sms, s);
+  return MG_OK;
 }
 
 // Flux sums of every cube of a batch: one block per unpadded pixel row of

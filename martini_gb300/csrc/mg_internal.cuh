@@ -205,7 +205,23 @@ struct Ws {
   unsigned* spec;        // [cap_spec] per-particle Gaussian spectra over [clo, chi], as the
                          // tensor-core form's scaled 16-bit hi | lo << 16 halves
   long long cap_spec;    // room in spec (the workspace beyond the fixed layout)
+  // Work queue order: item_order[k] is the k-th item the contraction takes,
+  // the items sorted by estimated cost, largest first (stable: equal costs
+  // keep segment order).  item_key / item_*_tmp are the sort's buffers.
+  int* item_order;       // [cap_items]
+  unsigned* item_key;    // [cap_items]
+  unsigned* item_key_tmp;
+  int* item_order_tmp;
+  long long cap_items;
 };
+
+// Upper bound on the work items of a binning with at most cap_pairs pairs:
+// every item holds at least one pair, and a segment of cnt pairs has
+// ceil(cnt / kch) <= 1 + cnt / KCH_MIN items.
+__host__ __device__ inline long long items_bound(long long nseg, long long cap_pairs) {
+  const long long b = nseg + cap_pairs / KCH_MIN + 1;
+  return cap_pairs < b ? cap_pairs : b;
+}
 
 // Host-side launchers (all asynchronous on stream s).
 void launch_set_gals(const Gal* gals, const Geo& g, const Ws& w, cudaStream_t s);
@@ -221,7 +237,7 @@ long long radix_blocks(long long n);
 bool launch_radix_sort(unsigned* keys, int* vals, unsigned* kt, int* vt, const long long* np,
                        long long cap, int bits, int* hist, long long* off, long long* sums,
                        int num_sms, cudaStream_t s);
-void launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
+int launch_contract_fp32(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
 int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
 void launch_reduce_partials(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);
 void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s);

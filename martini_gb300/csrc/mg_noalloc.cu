@@ -11,14 +11,23 @@
 // file-scope device array of MG_NOALLOC_SCRATCH_BYTES, reserved on every GPU
 // that loads the library for as long as the process lives.
 //
-// Set-up: the first call on a device (with that device current) looks the
-// array up with cudaGetSymbolAddress and caches the address; make that first
-// call before any stream capture.  Every call reuses the same array and the
-// pipeline re-initialises, on the device, everything that must start from
-// zero; two calls that overlap on the GPU (for example on two streams) race
-// on the array and corrupt each other.  The call synchronises the stream
-// (it reads back the status word) and allocates nothing: no cudaMalloc, no
-// cudaFree, no allocating library routine.
+// Set-up: every call (with the target device current) looks the array up
+// with cudaGetSymbolAddress, which allocates nothing and is cheap; nothing is
+// cached, so a device reset or a re-created primary context (which reloads
+// the module and may move the array) never leaves a stale address.  Every
+// call reuses the same array and the pipeline re-initialises, on the device,
+// everything that must start from zero; two calls that overlap on the GPU
+// (for example on two streams) race on the array and corrupt each other.
+// The call synchronises the stream (it reads back the status word), so it
+// cannot be captured in a CUDA graph, and it allocates nothing: no
+// cudaMalloc, no cudaFree, no allocating library routine.
+//
+// The array is shared out as: the fixed part of the workspace layout, then
+// (tensor-core forms with Gaussian lines) an eighth of the array held back
+// for the per-particle spectrum store, then a quarter of the rest for
+// split-K partial tiles and the largest (tile, particle) pair capacity that
+// fits.  A spectrum store that does not fit its share is skipped and the
+// lines are evaluated inside the contraction (same results).
 #include <string>
 
 #include "mg_internal.cuh"
@@ -31,23 +40,13 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MG_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array for the current device (looked up once
-// per device; the host-side symbol is not a device address).
+// Device address of the scratch array on the current device (the host-side
+// symbol is not a device address), looked up on every call.
 int scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return MG_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return MG_ERR_UNSUPPORTED;
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) return MG_ERR_CUDA;
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) return MG_ERR_CUDA;
+  *out = p;
   return MG_OK;
 }
 
@@ -61,7 +60,12 @@ extern "C" int mg_insert_noalloc(const mg_problem* p, void* stream) {
     mg::set_last_error("mg_insert_noalloc: cannot locate the device scratch array");
     return rc;
   }
-  const size_t cap = MG_NOALLOC_SCRATCH_BYTES;
+  // room held back for the spectrum store (tensor-core forms, Gaussian lines)
+  const bool tc = p->form == MG_FORM_BF16X3 || p->form == MG_FORM_F16X3 ||
+                  p->form == MG_FORM_BF16X6;
+  const size_t spec_room =
+      (tc && p->spectral_model == MG_SPECTRUM_GAUSSIAN) ? MG_NOALLOC_SCRATCH_BYTES / 8 : 0;
+  const size_t cap = MG_NOALLOC_SCRATCH_BYTES - spec_room;
   // capacities that fit the array: a quarter of what is left after the fixed
   // part goes to split-K partial tiles, the rest to the (tile, particle) list
   size_t fixed = 0;
@@ -89,7 +93,15 @@ extern "C" int mg_insert_noalloc(const mg_problem* p, void* stream) {
     if (rc) return rc;
     if (b <= cap) lo = mid; else hi = mid;
   }
-  rc = mg_insert(p, ws, cap, lo, cap_partial, stream);
+  rc = mg_insert(p, ws, MG_NOALLOC_SCRATCH_BYTES, lo, cap_partial, stream);
   if (rc) return rc;
-  return mg_check(ws, stream);
+  rc = mg_check(ws, stream);
+  if (rc == MG_ERR_WORKSPACE)
+    mg::set_last_error(
+        "mg_insert_noalloc: the built-in scratch (MG_NOALLOC_SCRATCH_BYTES = " +
+        std::to_string((size_t)MG_NOALLOC_SCRATCH_BYTES) +
+        " bytes) is too small for this problem's (tile, particle) pairs or split-K partial "
+        "tiles (room for " + std::to_string(lo) + " pairs and " + std::to_string(cap_partial) +
+        " partial tiles); use mg_insert with a workspace sized by mg_plan");
+  return rc;
 }

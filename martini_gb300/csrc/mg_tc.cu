@@ -5,21 +5,24 @@
 // 512 threads build in shared memory
 //   A = W[128 pixels][KC particles]        (kernel pixel integrals)
 //   B = S[Nw channels][KC particles]       (spectra over the stage's window)
-// each split into a hi + lo pair of 16-bit floats (bf16, or fp16 after exact
-// power-of-two scaling), stored K-major in the no-swizzle canonical layout
-// (8-row x 16-byte core matrices; K-direction stride 128 B, row-group stride
-// 256 B).  Thread 0 issues three tcgen05.mma (kind::f16, FP32 accumulate) per
-// 16-particle step -- W_hi S_hi + W_hi S_lo + W_lo S_hi -- into a TMEM
-// accumulator holding the tile's whole band (128 lanes = pixels, columns =
-// channels), at the stage's column window.  Two shared-memory stages
-// alternate: producers fill one while the tensor core reads the other, and
-// tcgen05.commit arrives on the stage's mbarrier when it may be reused.  The
-// records of the next stage travel global -> shared by cp.async while the
-// current one is produced.  Every two stages the working accumulator is
-// drained (round to nearest) into a master accumulator in the other half of
-// TMEM, halfway through the next stage's production.  The epilogue reads
-// TMEM with tcgen05.ld and writes 128-byte channel runs of each pixel to the
-// cube, or to a split-K partial buffer.
+// each split into 16-bit pieces: a hi + lo pair (bf16, or fp16 after exact
+// power-of-two scaling), or the exact three-piece BF16 split hi + mid + lo of
+// the FP32 value.  The pieces are stored K-major in the no-swizzle canonical
+// layout (8-row x 16-byte core matrices; K-direction stride 128 B, row-group
+// stride 256 B).  Thread 0 issues the products per 16-particle step -- three
+// for a pair (W_hi S_hi + W_hi S_lo + W_lo S_hi), six for three pieces (every
+// cross term down to 2^-16 relative: hh, hm, mh, mm, hl, lh) -- as
+// tcgen05.mma (kind::f16, FP32 accumulate) into a TMEM accumulator holding
+// the tile's whole band (128 lanes = pixels, columns = channels), at the
+// stage's column window.  Two shared-memory stages alternate: producers fill
+// one while the tensor core reads the other, and tcgen05.commit arrives on the
+// stage's mbarrier when it may be reused.  The records of the next stage
+// travel global -> shared by cp.async while the current one is produced.
+// Every two stages the working accumulator is drained (round to nearest) into
+// a master accumulator in the other half of TMEM, halfway through the next
+// stage's production.  The epilogue reads TMEM with tcgen05.ld and writes
+// 128-byte channel runs of each pixel to the cube, or to a split-K partial
+// buffer.
 //
 // Every mbarrier wait has an iteration limit: on expiry the kernel sets
 // ST_TIMEOUT, frees its TMEM and returns.
@@ -38,20 +41,39 @@ constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
 // The tensor core's FP32 accumulation does not round to nearest: summing
 // many MMAs into one accumulator drifts low (~2^-26 per MMA, relative).  When
 // the band fits in half of TMEM the working accumulator is drained every
-// TC_DRAIN stages into a master accumulator in the other half with
-// round-to-nearest FP32 adds, which bounds that drift to ~TC_DRAIN * 3 * KC/16
-// MMAs per partial sum.
+// TC_DRAIN stages (every stage for the three-piece split) into a master
+// accumulator in the other half with round-to-nearest FP32 adds, which bounds
+// that drift to the MMAs of one interval; within it the small cross terms
+// are issued before the hi x hi products.
 constexpr int TC_DRAIN = 2;
 // Radial tables up to this many cells (one float4 each, zero cells
 // included: every table of mg_kernel_tables.h) are copied to shared memory.
 constexpr int KT_SMEM_CELLS = 1025;
 constexpr int TC_MASTER_COL = 256;
-// Shared memory at the widest band: two stages of A and B hi/lo tiles
-// (KC = 64) plus the static arrays must fit in the 227 KB of a CTA.
-static_assert(2 * (2 * 4 * 4096 + 2 * 4 * TC_MASTER_COL * 32) + (KT_SMEM_CELLS + 257) * 16 +
-                      2 * 64 * (sizeof(PRec) + sizeof(int) + sizeof(long long)) + 4096 <=
-                  227 * 1024,
-              "tensor-core kernel shared memory");
+
+// Operand splits: a hi + lo pair of FP16 (scaled) or BF16 pieces, or three
+// BF16 pieces hi + mid + lo that represent the FP32 value exactly.
+constexpr int SPLIT_F16_2 = 0;
+constexpr int SPLIT_BF16_2 = 1;
+constexpr int SPLIT_BF16_3 = 2;
+__host__ __device__ constexpr int split_parts(int split) { return split == SPLIT_BF16_3 ? 3 : 2; }
+__host__ __device__ constexpr bool split_bf16(int split) { return split != SPLIT_F16_2; }
+// particles per stage: 64 for pairs, 32 for three pieces (the same bytes)
+__host__ __device__ constexpr int split_kc(int split) { return split == SPLIT_BF16_3 ? 32 : 64; }
+
+// Shared memory at the widest band: two stages of A and B pieces plus the
+// static arrays must fit in the 227 KB of a CTA.
+constexpr size_t tc_stage_bytes(int split, int nw) {
+  return (size_t)split_parts(split) * (split_kc(split) / 16) * (4096 + 32 * (size_t)nw);
+}
+constexpr size_t tc_static_bytes(int kc) {
+  return (KT_SMEM_CELLS + 257) * 16 + 2 * kc * (sizeof(PRec) + sizeof(int) + sizeof(long long)) +
+         4096;
+}
+static_assert(2 * tc_stage_bytes(SPLIT_F16_2, TC_MASTER_COL) + tc_static_bytes(64) <= 227 * 1024,
+              "tensor-core kernel shared memory (pairs)");
+static_assert(2 * tc_stage_bytes(SPLIT_BF16_3, TC_MASTER_COL) + tc_static_bytes(32) <= 227 * 1024,
+              "tensor-core kernel shared memory (three pieces)");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -306,6 +328,45 @@ __device__ __forceinline__ void split_pair(float a, float b, unsigned& hi, unsig
   }
 }
 
+// Exact three-piece BF16 split of two FP32 values, packed as (first |
+// second << 16) per piece.  hi keeps the top 16 bits of the float (sign,
+// exponent and 7 stored mantissa bits: a BF16 by truncation); r = v - hi is
+// exact (same sign and binade) and holds the remaining 16 mantissa bits; mid
+// is r truncated the same way and lo = r - mid is exact with at most 8
+// significant bits, so it is a BF16 too.  hi + mid + lo == v for every
+// normal float (the pieces carry the exponent range of FP32).
+__device__ __forceinline__ void split3_pair(float a, float b, unsigned& hi, unsigned& mid,
+                                            unsigned& lo) {
+  const unsigned ua = __float_as_uint(a), ub = __float_as_uint(b);
+  hi = __byte_perm(ua, ub, 0x7632);
+  const float ra = a - __uint_as_float(ua & 0xFFFF0000u);
+  const float rb = b - __uint_as_float(ub & 0xFFFF0000u);
+  const unsigned ura = __float_as_uint(ra), urb = __float_as_uint(rb);
+  mid = __byte_perm(ura, urb, 0x7632);
+  const float la = ra - __uint_as_float(ura & 0xFFFF0000u);
+  const float lb = rb - __uint_as_float(urb & 0xFFFF0000u);
+  lo = __byte_perm(__float_as_uint(la), __float_as_uint(lb), 0x7632);
+}
+
+// The pieces of two values (particles q, q + 1) stored at byte offset off of
+// each piece's tile; piece k's tile starts at base + k * piece_bytes.
+template <int SPLIT>
+__device__ __forceinline__ void store_split(float a, float b, unsigned char* base,
+                                            unsigned piece_bytes, unsigned off) {
+  if constexpr (SPLIT == SPLIT_BF16_3) {
+    unsigned h, m, l;
+    split3_pair(a, b, h, m, l);
+    *reinterpret_cast<unsigned*>(base + off) = h;
+    *reinterpret_cast<unsigned*>(base + piece_bytes + off) = m;
+    *reinterpret_cast<unsigned*>(base + 2 * piece_bytes + off) = l;
+  } else {
+    unsigned h, l;
+    split_pair<split_bf16(SPLIT)>(a, b, h, l);
+    *reinterpret_cast<unsigned*>(base + off) = h;
+    *reinterpret_cast<unsigned*>(base + piece_bytes + off) = l;
+  }
+}
+
 // Coefficients of table cell floor(u) (u >= 0) from shared memory, and the
 // fraction t: base32 is the shared address of the table minus 2^23 cells,
 // so the sum of 2^23 and floor(u) left in the float's bits by kt_floor's
@@ -471,13 +532,12 @@ __device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec*
 
 // A = W for particles (q, q + 1): lane l covers pixels l + 32 k, k = 0..3,
 // which share the column j = j0 + (l & 15).
-template <bool BF16>
+template <int SPLIT>
 __device__ __forceinline__ void produce_w_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
                                                const KSpec* ks, const float4* ktab,
                                                unsigned ktab_s32, int ktab_type,
                                                unsigned gtab_s32, int q, int i0, int j0, int lane,
-                                               float sw, unsigned char* a_hi,
-                                               unsigned char* a_lo) {
+                                               float sw, unsigned char* a0, unsigned a_bytes) {
   const int j = j0 + (lane & 15);
   const int ib = i0 + (lane >> 4);
   float w0[4], w1[4];
@@ -490,10 +550,7 @@ __device__ __forceinline__ void produce_w_pair(const PRec& r0, const PRec& r1, b
   for (int k = 0; k < 4; ++k) {
     const int p = lane + 32 * k;
     const unsigned off = qoff + (unsigned)(p >> 3) * 256u + (unsigned)(p & 7) * 16u;
-    unsigned hi, lo;
-    split_pair<BF16>(w0[k], w1[k], hi, lo);
-    *reinterpret_cast<unsigned*>(a_hi + off) = hi;
-    *reinterpret_cast<unsigned*>(a_lo + off) = lo;
+    store_split<SPLIT>(w0[k], w1[k], a0, a_bytes, off);
   }
 }
 
@@ -559,7 +616,7 @@ __device__ __forceinline__ unsigned spec_at(const SpecRow& q, int c) {
 // needs erfc at every window edge once: in step m lane l evaluates edge
 // 31 m + l and channel 31 m + l (l < 31) takes its upper index edge from
 // lane l + 1, so each step covers 31 channels with no repeated evaluation.
-template <bool BF16>
+template <int SPLIT>
 __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
                                                int q, int w0, int nw, int nc, int dec, int model,
                                                const float* ehi, const float* elo,
@@ -567,14 +624,14 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
                                                int pid0, int pid1, int lane, float ss,
                                                const unsigned* spec, long long soff0,
                                                long long soff1, unsigned pf0, unsigned pf1,
-                                               unsigned pf2, unsigned pf3, unsigned char* b_hi,
-                                               unsigned char* b_lo) {
+                                               unsigned pf2, unsigned pf3, unsigned char* b0,
+                                               unsigned b_bytes) {
   const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
                         (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
   if (spec) {
     // Gaussian lines read from the spectrum store, already scaled and split
-    // (hi | lo << 16 per value); the first 64 window channels were loaded
-    // before the weights
+    // (hi | lo << 16 per value; the FP32 value for three pieces); the first
+    // 64 window channels were loaded before the weights
     const SpecRow q0 = spec_row(spec, soff0, r0, v0), q1 = spec_row(spec, soff1, r1, v1);
     for (int base = 0; base < nw; base += 32) {  // warp-uniform
       const int n = base + lane;
@@ -592,8 +649,12 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
       }
       if (n < nw) {
         const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
-        *reinterpret_cast<unsigned*>(b_hi + off) = __byte_perm(s0, s1, 0x5410);
-        *reinterpret_cast<unsigned*>(b_lo + off) = __byte_perm(s0, s1, 0x7632);
+        if constexpr (SPLIT == SPLIT_BF16_3) {
+          store_split<SPLIT>(__uint_as_float(s0), __uint_as_float(s1), b0, b_bytes, off);
+        } else {
+          *reinterpret_cast<unsigned*>(b0 + off) = __byte_perm(s0, s1, 0x5410);
+          *reinterpret_cast<unsigned*>(b0 + b_bytes + off) = __byte_perm(s0, s1, 0x7632);
+        }
       }
     }
     return;
@@ -637,10 +698,7 @@ __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, b
     }
     if (n < nw && (!gauss || lane < 31)) {
       const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
-      unsigned hi, lo;
-      split_pair<BF16>(s0, s1, hi, lo);
-      *reinterpret_cast<unsigned*>(b_hi + off) = hi;
-      *reinterpret_cast<unsigned*>(b_lo + off) = lo;
+      store_split<SPLIT>(s0, s1, b0, b_bytes, off);
     }
   }
 }
@@ -685,6 +743,7 @@ __device__ __forceinline__ SpecIn spec_in(const Ws& w, long long p) {
 
 __global__ void k_spec_eval(Geo g, Ws w) {
   const bool form_bf16 = g.form == MG_FORM_BF16X3;
+  const bool form_fp32 = g.form == MG_FORM_BF16X6;  // the contraction splits the FP32 value
   const bool fits = w.hdr->n_spec <= w.cap_spec;
   // read by the contraction, which runs after this whole kernel
   if (blockIdx.x == 0 && threadIdx.x == 0) w.hdr->spec_ready = fits ? 1 : 0;
@@ -716,7 +775,7 @@ __global__ void k_spec_eval(Geo g, Ws w) {
         ehi = w.ehi + G.edge0;
         elo = w.elo + G.edge0;
         inv_w = w.inv_w + G.edge0;
-        ss = form_bf16 ? 1.f : spec_scale(w.gst[gk_c], g.spectral_model);
+        ss = (form_bf16 || form_fp32) ? 1.f : spec_scale(w.gst[gk_c], g.spectral_model);
       }
       PRec r;
       r.vhi = cur.vhi;
@@ -734,8 +793,10 @@ __global__ void k_spec_eval(Geo g, Ws w) {
         if (lane < 31 && m < cnt) {
           const float phi =
               dec ? half_diff_from_c(cb, pb, ca, pa) : half_diff_from_c(ca, pa, cb, pb);
-          out[m] = form_bf16 ? split_one<true>((cur.amp * inv_w[c] * phi) * ss)
-                             : split_one<false>((cur.amp * inv_w[c] * phi) * ss);
+          const float val = (cur.amp * inv_w[c] * phi) * ss;
+          out[m] = form_fp32   ? __float_as_uint(val)
+                   : form_bf16 ? split_one<true>(val)
+                               : split_one<false>(val);
         }
       }
     }
@@ -759,10 +820,17 @@ __device__ __forceinline__ void window_partial(int (*win)[2], const PRec& r, boo
   }
 }
 
-template <bool BF16, int KC>
+template <int SPLIT, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
-  static_assert(KC == 64, "records of a stage: warps 0 and 1, one per thread");
+  static_assert(KC == split_kc(SPLIT), "stage size of the split");
+  static_assert(KC == 32 || KC == 64, "records of a stage: one per thread of warps 0 (and 1)");
+  constexpr bool BF16 = split_bf16(SPLIT);
+  constexpr int NP = split_parts(SPLIT);  // 16-bit pieces per operand
+  constexpr int RWARPS = KC / 32;         // warps that copy a stage's records
+  // stages between drains: TC_DRAIN for pairs (24 MMAs), every stage for
+  // three pieces (the same 24 MMAs, over half the particles)
+  constexpr int DRAIN_STAGES = NP == 3 ? 1 : TC_DRAIN;
   constexpr int KSTEPS = KC / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(16) PRec recs[2][KC];
@@ -788,9 +856,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
                           ? w.spec
                           : nullptr;
 
-  const unsigned a_bytes = KSTEPS * 4096u;
-  const unsigned b_bytes = KSTEPS * (unsigned)nwmax * 32u;
-  const unsigned st_bytes = 2u * a_bytes + 2u * b_bytes;
+  const unsigned a_bytes = KSTEPS * 4096u;                 // one piece of A
+  const unsigned b_bytes = KSTEPS * (unsigned)nwmax * 32u;  // one piece of B
+  const unsigned st_bytes = NP * (a_bytes + b_bytes);
   const unsigned sbase = smem_u32(smem);
 
   if (tid < MG_MAX_KERNELS) s_ks[tid] = g.ks[tid];
@@ -884,7 +952,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     __syncthreads();
     const long long item = s_item;
     if (item >= n_items || s_abort) break;
-    const ItemTC it = decode_tc(g, w, item, kch);
+    // the queue runs over the items in cost order, largest first
+    const ItemTC it = decode_tc(g, w, (long long)w.item_order[item], kch);
     const Gal& G = w.gal[it.gal];
     const GalState& gs = w.gst[it.gal];
     const int dec = gs.dec;
@@ -959,10 +1028,12 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       // stage channel window [w0, w0 + nw): min clo, max chi
       int w0, nw;
       {
-        // the two halves' extremes, reduced by warps 0 and 1 when the
-        // records arrived
-        int lo = min(s_win[buf][0][0], s_win[buf][1][0]);
-        int hi = max(s_win[buf][0][1], s_win[buf][1][1]);
+        // the extremes reduced by the record warps when the records arrived
+        int lo = s_win[buf][0][0], hi = s_win[buf][0][1];
+        if (RWARPS > 1) {
+          lo = min(lo, s_win[buf][1][0]);
+          hi = max(hi, s_win[buf][1][1]);
+        }
         // relative to the segment's block [c0, c0 + ncols)
         lo = max(lo, it.c0) - it.c0;
         hi = min(hi, it.c0 + ncols - 1) - it.c0;
@@ -978,25 +1049,29 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         t_lo = min(t_lo, w0);
         t_hi = max(t_hi, w0 + nw);
       }
-      unsigned char* const sa_hi = smem + stage * st_bytes;
-      unsigned char* const sa_lo = sa_hi + a_bytes;
-      unsigned char* const sb_hi = sa_lo + a_bytes;
-      unsigned char* const sb_lo = sb_hi + b_bytes;
+      unsigned char* const sa = smem + stage * st_bytes;  // NP pieces of A, then of B
+      unsigned char* const sb = sa + NP * a_bytes;
+      // drain of the previous interval: the MMAs of the previous stage are
+      // waited for, then the working accumulator is added into the master
+      auto drain_now = [&]() {
+        const int sp = stage ^ 1;  // the previous stage's buffer
+        if (!mbar_wait(smem_u32(&bars[sp]), (phase_bits >> sp) & 1u)) s_abort = 1;
+        phase_bits ^= 1u << sp;
+        pending_bits &= ~(1u << sp);
+        tc_fence_after();
+        drain_tmem(p_lo, p_hi);
+        tc_fence_before();
+        drain_due = false;
+      };
       // ---- A = W and B = S, particle-major: warp w owns particles
       // w * PPW .. w * PPW + PPW - 1, taken in pairs
       constexpr int PPW = KC / (TC_THREADS / 32);
+      // the drain runs halfway through this stage's production (after it,
+      // for one pair per warp)
+      constexpr int DRAIN_PP = PPW >= 4 ? PPW / 2 : PPW;
 #pragma unroll
       for (int pp = 0; pp < PPW; pp += 2) {
-        if (pp == PPW / 2 && drain_due) {  // warp-uniform
-          const int sp = stage ^ 1;  // the previous stage's buffer
-          if (!mbar_wait(smem_u32(&bars[sp]), (phase_bits >> sp) & 1u)) s_abort = 1;
-          phase_bits ^= 1u << sp;
-          pending_bits &= ~(1u << sp);
-          tc_fence_after();
-          drain_tmem(p_lo, p_hi);
-          tc_fence_before();
-          drain_due = false;
-        }
+        if (pp == DRAIN_PP && drain_due) drain_now();  // warp-uniform
         const int q = warp * PPW + pp;
         const PRec r0 = recs[buf][q];
         const PRec r1 = recs[buf][q + 1];
@@ -1017,14 +1092,15 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
           pf2 = spec_at(q0, wa + 32 + lane);
           pf3 = spec_at(q1, wa + 32 + lane);
         }
-        produce_w_pair<BF16>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type,
-                             smem_u32(s_gtab), q, i0, j0, lane, sw, sa_hi, sa_lo);
-        produce_s_pair<BF16>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
-                             w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
-                             (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0), lane,
-                             ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf0, pf1, pf2, pf3, sb_hi,
-                             sb_lo);
+        produce_w_pair<SPLIT>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type,
+                              smem_u32(s_gtab), q, i0, j0, lane, sw, sa, a_bytes);
+        produce_s_pair<SPLIT>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
+                              w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
+                              (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0),
+                              lane, ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf0, pf1, pf2,
+                              pf3, sb, b_bytes);
       }
+      if (DRAIN_PP == PPW && drain_due) drain_now();
       if (has_next && tid < KC) {
         cp_async_wait_all();
         window_partial(s_win[buf ^ 1], recs[buf ^ 1][tid], k0 + KC + tid < it.lcount, warp, lane);
@@ -1039,24 +1115,44 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         // K-step offsets: every stage address is below 256 KB, so no carry.
         const unsigned base = sbase + stage * st_bytes;
         const unsigned id = idesc_f16kind(128, nw, BF16);
+        // pieces: hi, lo (pairs) or hi, mid, lo (three), a_bytes / b_bytes apart
         const unsigned long long a_hi = sdesc(base, 128, 256);
-        const unsigned long long a_lo = a_hi + (a_bytes >> 4);
-        const unsigned long long b_hi = sdesc(base + 2u * a_bytes, 128, 256);
-        const unsigned long long b_lo = b_hi + (b_bytes >> 4);
+        const unsigned long long a_2 = a_hi + (a_bytes >> 4);
+        const unsigned long long b_hi = sdesc(base + NP * a_bytes, 128, 256);
+        const unsigned long long b_2 = b_hi + (b_bytes >> 4);
         const unsigned bstep = (unsigned)nw * 2u;  // K step of B: nw * 32 bytes
         const unsigned d = tmem + (unsigned)w0;
+        // Smallest terms first: the tensor core's FP32 accumulation truncates
+        // each MMA's sum to the accumulator's precision, so every MMA loses up
+        // to an ulp of the accumulator.  Issued into the working accumulator
+        // the last drain left at zero, the cross terms (2^-8 .. 2^-16 of the
+        // hi products) lose ulps of their own small sums; only the hi x hi
+        // products, last, meet the full-size accumulator.
+        if constexpr (NP == 3) {
+          const unsigned long long a_3 = a_2 + (a_bytes >> 4);
+          const unsigned long long b_3 = b_2 + (b_bytes >> 4);
+#pragma unroll
+          for (int ks = 0; ks < KSTEPS; ++ks) {
+            const unsigned ao = (unsigned)ks * 256u, bo = (unsigned)ks * bstep;
+            umma(d, a_2 + ao, b_2 + bo, id, 1u);   // mid mid
+            umma(d, a_hi + ao, b_3 + bo, id, 1u);  // hi lo
+            umma(d, a_3 + ao, b_hi + bo, id, 1u);  // lo hi
+          }
+        }
 #pragma unroll
         for (int ks = 0; ks < KSTEPS; ++ks) {
           const unsigned ao = (unsigned)ks * 256u, bo = (unsigned)ks * bstep;
-          umma(d, a_hi + ao, b_hi + bo, id, 1u);
-          umma(d, a_hi + ao, b_lo + bo, id, 1u);
-          umma(d, a_lo + ao, b_hi + bo, id, 1u);
+          umma(d, a_hi + ao, b_2 + bo, id, 1u);  // hi lo (pair) / hi mid
+          umma(d, a_2 + ao, b_hi + bo, id, 1u);  // lo hi (pair) / mid hi
         }
+#pragma unroll
+        for (int ks = 0; ks < KSTEPS; ++ks)
+          umma(d, a_hi + (unsigned)ks * 256u, b_hi + (unsigned)ks * bstep, id, 1u);
         umma_commit(smem_u32(&bars[stage]));
       }
       pending_bits |= 1u << stage;
       stage ^= 1;
-      if (drain && ++since_drain == TC_DRAIN && ch + 1 < nchunk) {
+      if (drain && ++since_drain == DRAIN_STAGES && ch + 1 < nchunk) {
         // drain the interval's columns during the next stage (its commit
         // covers every earlier MMA)
         drain_due = true;
@@ -1167,10 +1263,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   }
 }
 
-template <bool BF16, int KC>
+template <int SPLIT>
 int launch_tc(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, int nwmax) {
-  constexpr int KSTEPS = KC / 16;
-  size_t smem = 2 * (2 * (size_t)KSTEPS * 4096 + 2 * (size_t)KSTEPS * nwmax * 32);
+  constexpr int KC = split_kc(SPLIT);
+  size_t smem = 2 * tc_stage_bytes(SPLIT, nwmax);
   // at least 116 KB so that one CTA (and its 512 TMEM columns) fits per SM
   if (smem < 118784) smem = 118784;
   // the shared-memory attribute is per device: set once on each (host-side
@@ -1181,15 +1277,15 @@ int launch_tc(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, int nwmax)
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return MG_ERR_CUDA;
   if (attr_bytes[dev] <= 0) {
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, k_contract_tc<BF16, KC>) != cudaSuccess) return MG_ERR_CUDA;
+    if (cudaFuncGetAttributes(&fa, k_contract_tc<SPLIT, KC>) != cudaSuccess) return MG_ERR_CUDA;
     const int bytes = 227 * 1024 - (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute(k_contract_tc<BF16, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_contract_tc<SPLIT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              bytes) != cudaSuccess)
       return MG_ERR_CUDA;
     attr_bytes[dev] = bytes;
   }
   if ((int)smem > attr_bytes[dev]) return MG_ERR_UNSUPPORTED;
-  k_contract_tc<BF16, KC><<<num_sms, TC_THREADS, smem, s>>>(g, w, nwmax);
+  k_contract_tc<SPLIT, KC><<<num_sms, TC_THREADS, smem, s>>>(g, w, nwmax);
   return MG_OK;
 }
 
@@ -1210,9 +1306,9 @@ void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
 int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
   const int nwmax = g.max_width;  // a stage window never exceeds the widest block
   if (nwmax > TC_MASTER_COL) return MG_ERR_UNSUPPORTED;
-  const bool bf16 = g.form == MG_FORM_BF16X3;
-  const int rc = bf16 ? launch_tc<true, 64>(g, w, num_sms, s, nwmax)
-                      : launch_tc<false, 64>(g, w, num_sms, s, nwmax);
+  const int rc = g.form == MG_FORM_BF16X6   ? launch_tc<SPLIT_BF16_3>(g, w, num_sms, s, nwmax)
+                 : g.form == MG_FORM_BF16X3 ? launch_tc<SPLIT_BF16_2>(g, w, num_sms, s, nwmax)
+                                            : launch_tc<SPLIT_F16_2>(g, w, num_sms, s, nwmax);
   if (rc) return rc;
   launch_reduce_partials(g, w, num_sms, s);
   return MG_OK;

@@ -20,13 +20,17 @@ from .engine import DeviceParticles, InsertionEngine
 
 MHI_TO_JY = 2.36e5  # Msun / (Mpc^2 Jy km/s), martini/spectral_models.py:127-145
 
-FORMS = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3}
+FORMS = {"fp32": N.MG_FORM_FP32, "bf16x3": N.MG_FORM_BF16X3, "f16x3": N.MG_FORM_F16X3,
+         "bf16x6": N.MG_FORM_BF16X6}
+# the chosen form: exact three-piece BF16 split on the tensor cores, within
+# 1e-5 of peak and 1e-6 of flux of the FP64 reference arithmetic
+DEFAULT_FORM = "bf16x6"
 
 
 class _BaseMartini:
     def __init__(self, *, source, datacube: DataCube, beam=None, noise=None, sph_kernel,
                  spectral_model, quiet: bool = False, _prune_kwargs: dict | None = None,
-                 form: str = "fp32", device=None):
+                 form: str = DEFAULT_FORM, device=None):
         self.quiet = quiet
         self.source = source
         self._datacube = datacube
@@ -169,13 +173,16 @@ class _BaseMartini:
 class Martini(_BaseMartini):
     """Synthetic HI data cubes from SPH particles, inserted on the GPU.
 
-    Same constructor as the reference plus two keywords: ``form`` ("fp32",
-    the FP32 CUDA-core contraction, or "bf16x3", the BF16 hi+lo tensor-core
-    form) and ``device``.
+    Same constructor as the reference plus two keywords: ``form`` and
+    ``device``.  ``form`` selects the contraction: "bf16x6" (default; the
+    exact three-piece BF16 split, six tensor-core products), "f16x3" (scaled
+    FP16 hi + lo, three products), "fp32" (FP32 on CUDA cores) or "bf16x3"
+    (BF16 hi + lo, three products: about 1e-5 relative per term, so it can
+    miss the 1e-5-of-peak bar on cubes dominated by a few particles).
     """
 
     def __init__(self, *, source, datacube, beam=None, noise=None, sph_kernel, spectral_model,
-                 quiet: bool = False, form: str = "fp32", device=None):
+                 quiet: bool = False, form: str = DEFAULT_FORM, device=None):
         super().__init__(source=source, datacube=datacube, beam=beam, noise=noise,
                          sph_kernel=sph_kernel, spectral_model=spectral_model, quiet=quiet,
                          form=form, device=device)

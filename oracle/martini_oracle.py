@@ -29,6 +29,7 @@ Two insertion forms are provided:
 from __future__ import annotations
 
 import math
+import os
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -658,3 +659,113 @@ def incline(xyz, vxyz, incl_deg):
     Ry = np.array([[np.cos(i), 0, np.sin(i)], [0, 1, 0], [-np.sin(i), 0, np.cos(i)]])
     M = Ry @ M0
     return xyz @ M.T, vxyz @ M.T
+
+
+# ---------------------------------------------------------------------------
+# Total flux per particle in C (FP64), for full-size parity
+# ---------------------------------------------------------------------------
+
+_CLIB = None
+
+
+def _clib():
+    """The oracle's C restatement (oracle/flux_total.c), built on first use."""
+    global _CLIB
+    if _CLIB is None:
+        import ctypes as C
+        from oracle import build as ob
+        lib = C.CDLL(ob.build())
+        dp = C.POINTER(C.c_double)
+        lib.mgo_flux_total.restype = C.c_double
+        lib.mgo_flux_total.argtypes = [C.c_int64, dp, dp, dp, dp, C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_int), dp, dp, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, C.c_void_p]
+        lib.mgo_spectrum_sums.restype = None
+        lib.mgo_spectrum_sums.argtypes = [C.c_int64, dp, C.c_void_p, C.c_double, dp, C.c_int,
+                                          C.c_int, dp, C.c_int, dp]
+        _CLIB = lib
+    return _CLIB
+
+
+def _f64(a):
+    import ctypes as C
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def spectrum_sums(model: str, v_kms, sigma_kms, amp, edges_kms, threads=None):
+    """sum_c S_p(c) per particle in Jy, S_p(c) = amp_p phi_p(c) / |dv_c|
+    (spectral_models.py:63-200; Gaussian :386-425, Dirac :544-570), in
+    FP64 C.  ``sigma_kms`` is an array or a scalar (Gaussian only)."""
+    import ctypes as C
+    lib = _clib()
+    v, vp = _f64(v_kms)
+    a, ap = _f64(np.broadcast_to(amp, v.shape))
+    e, ep = _f64(edges_kms)
+    out = np.empty(v.shape[0])
+    sig_arr, sig_ptr, sig_c = None, None, 0.0
+    if model == "gaussian":
+        if np.ndim(sigma_kms) == 0:
+            sig_c = float(sigma_kms)
+        else:
+            sig_arr, _ = _f64(sigma_kms)
+            sig_ptr = sig_arr.ctypes.data_as(C.c_void_p)
+    lib.mgo_spectrum_sums(v.shape[0], vp, sig_ptr, sig_c, ap, 1 if model == "dirac" else 0,
+                          e.shape[0] - 1, ep, threads or os.cpu_count() or 1,
+                          out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def flux_total(x, y, ranges, kernels, kidx, h_eff, ssum, nx, ny, padx=0, pady=0,
+               threads=None, return_wsum=False):
+    """Total flux over the unpadded cube, sum_p (sum_box W_p) (sum_c S_p(c)),
+    in FP64 C: the reference's per-pixel sums (martini/martini.py:243-283)
+    added over the unpadded pixels (:367-375), reordered per particle.
+    ``ssum`` comes from :func:`spectrum_sums`."""
+    import ctypes as C
+    lib = _clib()
+    xs, xp = _f64(x)
+    ys, yp = _f64(y)
+    rs, rp = _f64(ranges)
+    hs, hp = _f64(h_eff)
+    ss, sp = _f64(ssum)
+    n = xs.shape[0]
+    ki = None if kidx is None else np.ascontiguousarray(kidx, dtype=np.int8)
+    kt = (C.c_int * 4)(*[int(k["ktype"]) for k in kernels] + [0] * (4 - len(kernels)))
+    tr = np.array([float(k.get("truncate", 3.0)) for k in kernels] + [3.0] * (4 - len(kernels)))
+    wsum = np.empty(n) if return_wsum else None
+    tot = lib.mgo_flux_total(n, xp, yp, rp, hp,
+                             None if ki is None else ki.ctypes.data_as(C.c_void_p),
+                             len(kernels), kt, tr.ctypes.data_as(C.POINTER(C.c_double)), sp,
+                             int(nx), int(ny), int(padx), int(pady),
+                             threads or os.cpu_count() or 1,
+                             None if wsum is None else wsum.ctypes.data_as(C.c_void_p))
+    return (tot, wsum) if return_wsum else tot
+
+
+def pixel_spectra(pixels, x, y, ranges, kernels, kidx, h_eff, model, mHI, dist, v, edges,
+                  sigma=None, threads=8):
+    """The reference's per-pixel sum (``_evaluate_pixel_spectrum``,
+    martini/martini.py:243-283) at each (i, j) of ``pixels``, FP64: the
+    Chebyshev-box mask over all particles, the kernel weights of the masked
+    ones (sph_kernels.py:85-119) and their spectra (spectral_models.py:63-200).
+    Returns an array [len(pixels), nc] in Jy / pix^2."""
+    nc = len(edges) - 1
+    kidx = np.zeros(x.shape[0], np.int64) if kidx is None else np.asarray(kidx, np.int64)
+    h_eff = np.asarray(h_eff, np.float64)
+
+    def one(ij):
+        i, j = ij
+        m = (np.abs(x - i) <= ranges) & (np.abs(y - j) <= ranges)
+        if not m.any():
+            return np.zeros(nc)
+        dij = np.vstack((x[m] - i, y[m] - j))
+        wt = px_weight(kernels, kidx[m], dij, h_eff[m])
+        sig = None
+        if model == "gaussian":
+            sig = np.broadcast_to(np.asarray(sigma, np.float64), x.shape)[m]
+        sp = init_spectra(model, mHI[m], dist[m], v[m], edges, sig)
+        return wt @ sp
+
+    with ThreadPoolExecutor(threads) as ex:
+        return np.stack(list(ex.map(one, pixels)))

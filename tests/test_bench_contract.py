@@ -25,8 +25,10 @@ def test_reference_arm_line():
     assert KEYS <= set(d)
     assert d["impl"] == "reference" and d["unit"] == "cubes/s" and d["value"] > 0
     assert d["higher_is_better"] is True and d["vs_baseline"] is None
-    assert d["config"]["workload"] == "disc1m_512" and d["config"]["particles"] > 0
+    assert d["config"]["workload"] == "disc4m_1024" and d["config"]["particles"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    # a bounded pixel sample scaled to a whole cube, flagged as such
+    assert cb["extrapolated"] is True and 0 < cb["timed_fraction"] < 1
     assert d["e2e"] == {"value": d["value"], "unit": "cubes/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}

@@ -1,7 +1,10 @@
 """GPU parity: the CUDA insertion against the reference's golden cubes and
 the FP64 oracle.  Tolerances: max |cube - ref| / peak(ref) <= 1e-5 and
-|flux - ref flux| / ref flux <= 1e-6 (FP32 and FP16-split forms; the BF16
-split is held to its per-term bound, below)."""
+|flux - ref flux| / ref flux <= 1e-6 for every form that claims them: FP32,
+the scaled FP16 split (f16x3) and the exact three-piece BF16 split (bf16x6).
+The two-piece BF16 split (bf16x3, ~16 bits per operand) is checked against
+the same bar in an expected-failure test: it meets it on most cubes but not
+on every one."""
 
 import numpy as np
 import pytest
@@ -49,18 +52,13 @@ def assert_close(got, ref, flux=None, pad=0, tol=TOL_PEAK, ftol=TOL_FLUX):
                                    atol=1e-6 * np.abs(ref[sl].sum(axis=(0, 1))).max())
 
 
-FORMS = [0, 1, 2]  # MG_FORM_FP32, MG_FORM_BF16X3, MG_FORM_F16X3
-FORM_IDS = ["fp32", "bf16x3", "f16x3"]
-# the BF16 hi+lo split keeps ~16 mantissa bits: per term 3 * 2^-18 = 1.1e-5
-# relative in the worst case, so a voxel dominated by one particle can miss
-# 1e-5 of the peak; FP32 and the scaled FP16 split (3 * 2^-22) are held to it
-FORM_TOL = {0: 1e-5, 1: 2e-5, 2: 1e-5}
-# The flux of a cube carries the same per-term error: well below 1e-6 when
-# many voxels contribute, but a small cube dominated by a few one-particle
-# voxels can be off by up to the BF16 split's 3 * 2^-18 (measured 2.1e-6 on
-# the 16 x 16 WendlandC6 golden cube, whose three brightest voxels hold
-# most of the flux).  FP32 and the scaled FP16 split keep 1e-6.
-FLUX_TOL = {0: TOL_FLUX, 1: 1.2e-5, 2: TOL_FLUX}
+# MG_FORM_FP32, MG_FORM_F16X3, MG_FORM_BF16X6: every form held to the bar
+FORMS = [0, 2, 3]
+FORM_IDS = ["fp32", "f16x3", "bf16x6"]
+FORM_TOL = {0: TOL_PEAK, 2: TOL_PEAK, 3: TOL_PEAK}
+FLUX_TOL = {0: TOL_FLUX, 2: TOL_FLUX, 3: TOL_FLUX}
+TC_FORMS = [2, 3]
+TC_IDS = ["f16x3", "bf16x6"]
 
 
 @pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
@@ -71,6 +69,26 @@ def test_golden_cube(engine, case, form):
     assert len(c["x"]) == int(d["n_after"])
     got, flux = run_gpu(engine, c, form=form)
     assert_close(got, d["cube"], flux, c["pad"], tol=FORM_TOL[form], ftol=FLUX_TOL[form])
+
+
+@pytest.mark.xfail(strict=False, reason="the two-piece BF16 split keeps ~16 bits per operand "
+                   "(up to 3 * 2^-18 = 1.1e-5 relative per term): a cube whose peak or flux "
+                   "sits in a few one-particle voxels can miss 1e-5 of peak / 1e-6 of flux")
+def test_golden_cubes_bf16x3_at_the_bar(engine):
+    """MG_FORM_BF16X3 against every golden cube at the real bar."""
+    worst = []
+    for case in golden_cases():
+        d = load_case(case)
+        c = case_inputs(d)
+        got, flux = run_gpu(engine, c, form=1)
+        ref = d["cube"]
+        peak = np.abs(ref).max()
+        pad = c["pad"]
+        tot = ref[pad:ref.shape[0] - pad, pad:ref.shape[1] - pad].sum()
+        worst.append((np.abs(got - ref).max() / peak, abs(flux[0] - tot) / tot, case))
+    e, f, case = max(worst)
+    assert e <= TOL_PEAK, f"{case}: max err / peak {e:.3e}"
+    assert max(w[1] for w in worst) <= TOL_FLUX
 
 
 def test_martini_api_matches_oracle():
@@ -256,7 +274,7 @@ def test_split_k_large_tile_matches_oracle(engine, form):
     assert_close(got, ref, flux, tol=FORM_TOL[form], ftol=FLUX_TOL[form])
 
 
-@pytest.mark.parametrize("form", [1, 2], ids=["bf16x3", "f16x3"])
+@pytest.mark.parametrize("form", TC_FORMS, ids=TC_IDS)
 def test_spectrum_store_matches_in_kernel_lines(engine, form):
     """The tensor-core forms read Gaussian lines from the per-particle
     spectrum store when the workspace has room for it (mg_plan's size) and
@@ -297,7 +315,7 @@ def test_spectrum_store_matches_in_kernel_lines(engine, form):
     np.testing.assert_array_equal(cubes[0], cubes[1])
 
 
-@pytest.mark.parametrize("form", [0, 2], ids=["fp32", "f16x3"])
+@pytest.mark.parametrize("form", FORMS, ids=FORM_IDS)
 @pytest.mark.parametrize("shape", [(2048, 2048), (4096, 2048)], ids=["2048x2048", "4096x2048"])
 def test_large_sparse_tile_grids(engine, shape, form):
     """Tile grids too large for the shared-memory coverage histogram of the
@@ -460,7 +478,7 @@ def test_cuda_graph_replay_matches_direct_run(engine):
                                       v=rng.normal(200, 30, n), sigma=rng.uniform(4, 10, n),
                                       amp=10 ** rng.uniform(-7, -6, n))
     edges = torch.from_numpy(orc.vrad_channel_edges(nc, 4.0, 200.0)).to(engine.device)
-    for form in (N.MG_FORM_FP32, N.MG_FORM_F16X3):
+    for form in (N.MG_FORM_FP32, N.MG_FORM_F16X3, N.MG_FORM_BF16X6):
         eng = InsertionEngine("cuda:0")
         cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=eng.device)
         flux = torch.empty(nc + 1, dtype=torch.float64, device=eng.device)
