@@ -92,6 +92,8 @@ def parse():
                     help="skip timing the plain FP32 form beside the chosen form")
     ap.add_argument("--no-errors", action="store_true",
                     help="skip the error fields against the FP64 oracle")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="use the default launch shape instead of autotuning it")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end leg (its second buffer set): for profiling")
     ap.add_argument("--n-gal", type=int, default=200,
@@ -269,9 +271,10 @@ def band_workload(w, rank, world):
     return sub
 
 
-def build_insertions(w, form, dev, edges, cube, flux):
+def build_insertions(w, form, dev, edges, cube, flux, tune=False):
     """One planned insertion per spectral group of the workload; groups after
-    the first add to the cube."""
+    the first add to the cube.  With ``tune`` each insertion's launch shape is
+    autotuned (mg_tune) and cached before any timed or captured run."""
     from martini_gb300.engine import DeviceParticles, InsertionEngine
     groups = w["groups"] or [dict(sel=None, spectral_model=w["spectral_model"])]
     ins = []
@@ -287,7 +290,8 @@ def build_insertions(w, form, dev, edges, cube, flux):
                            w["ny"], w["nc"], 0, 0, edges, cube, flux, form,
                            accumulate=gi > 0)
         info = eng.plan(prob)
-        ins.append(dict(eng=eng, parts=parts, prob=prob, info=info, s=s))
+        shape = eng.tune(prob, reps=2) if tune else None
+        ins.append(dict(eng=eng, parts=parts, prob=prob, info=info, s=s, shape=shape))
     return ins
 
 
@@ -398,7 +402,7 @@ def main():
     nx, ny, nc = w["nx"], w["ny"], w["nc"]
     cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=dev)
     flux = torch.empty(nc + 1, dtype=torch.float64, device=dev)
-    ins = build_insertions(w, form, dev, edges, cube, flux)
+    ins = build_insertions(w, form, dev, edges, cube, flux, tune=not a.no_tune)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     graph = graph_of(ins)
@@ -444,7 +448,8 @@ def main():
     if form != FORMS["fp32"] and not a.no_fp32 and world == 1:
         cube32 = torch.empty_like(cube)
         flux32 = torch.empty_like(flux)
-        ins32 = build_insertions(w, FORMS["fp32"], dev, edges, cube32, flux32)
+        ins32 = build_insertions(w, FORMS["fp32"], dev, edges, cube32, flux32,
+                                 tune=not a.no_tune)
         g32 = graph_of(ins32)
         flush.zero_()
         g32.replay()
@@ -506,7 +511,9 @@ def main():
                    "kernel": w_full["kernel_name"], "spectrum": w_full["spectral_kind"],
                    "form": a.form, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"bands{world}" if world > 1 else "single",
-                   "pairs": int(sum(g["info"].n_pairs for g in ins)), "groups": len(ins)},
+                   "pairs": int(sum(g["info"].n_pairs for g in ins)), "groups": len(ins),
+                   "launch_shape": [g["shape"] for g in ins] if not a.no_tune
+                   else "default (not tuned)"},
         "particle_channel_updates_per_s": updates * a.steps / t_steps,
         "spectrum_evaluations_per_s": float(w_full["n"]) * w_full["nc"] * a.steps / t_steps,
         "errors": err,
@@ -655,6 +662,7 @@ def run_population(a, rank, world, local, dev):
         probs.append(prob)
     batch = BatchInsertion(eng, probs, keep=items)
     info = batch.plan()
+    shape = batch.tune(reps=2) if not a.no_tune else None
     # looped plain form: one mg_insert per cube on one shared workspace
     loop_eng = InsertionEngine(dev)
     caps = []
@@ -669,6 +677,22 @@ def run_population(a, rank, world, local, dev):
         for prob, cp in zip(probs, caps):
             N.check(loop_eng.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
                                            cp[0], cp[1], C.c_void_p(stream.cuda_stream)))
+
+    # the plain FP32 form looped over the same cubes
+    probs32, caps32 = [], []
+    loop32 = InsertionEngine(dev)
+    for prob in probs:
+        q = N.Problem.from_buffer_copy(prob)
+        q.form = FORMS["fp32"]
+        loop32.plan(q)
+        probs32.append(q)
+        caps32.append(loop32._caps)
+
+    def looped_fp32():
+        ws = loop32._ws
+        for prob, cp in zip(probs32, caps32):
+            N.check(loop32.lib.mg_insert(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                         cp[0], cp[1], C.c_void_p(stream.cuda_stream)))
 
     def timed(fn, k):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -699,6 +723,8 @@ def run_population(a, rank, world, local, dev):
     clk = clocks.stop()
     batch.check()
     t_loop = timed(looped, a.steps)
+    looped_fp32()
+    t_loop32 = timed(looped_fp32, max(1, min(a.steps, 3)))
     batch.run_stages(N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
     t_contract = float(np.mean(timed(lambda: batch.run_stages(N.MG_STAGE_CONTRACT), 3)))
     # end to end: particles from pinned host memory, every cube back.  Two
@@ -817,10 +843,14 @@ def run_population(a, rank, world, local, dev):
                    "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"lpt{world}" if world > 1 else "single",
                    "pairs_rank0": int(info.n_pairs), "form_batched": True,
-                   "lpt_imbalance": imbalance},
+                   "lpt_imbalance": imbalance,
+                   "launch_shape": shape if shape else "default (not tuned)"},
         "looped": {"value": ng * a.steps / tl, "unit": "cubes/s",
                    "ms_per_step": tl / a.steps * 1e3,
-                   "note": "same cubes, one mg_insert per cube"},
+                   "note": f"same cubes, one mg_insert per cube, {a.form}"},
+        "looped_fp32": {"value": ng * len(t_loop32) / float(np.sum(t_loop32)),
+                        "unit": "cubes/s", "ms_per_step": float(np.mean(t_loop32)) * 1e3,
+                        "note": "same cubes, one mg_insert per cube, plain FP32 form"},
         "particle_channel_updates_per_s": updates * a.steps / tb,
         "spectrum_evaluations_per_s": float(sum(w["n"] * w["nc"] for w in gals_all)) * a.steps
                                       / tb,

@@ -202,6 +202,62 @@ int mg_insert_stages_batched(const mg_problem* probs, int32_t nprob, void* works
                              int32_t stages, void* stream);
 
 /*
+ * Launch shape of an insertion and its autotuner.  No counterpart in the
+ * reference, whose only scheduling knob is the pixel thread pool
+ * (martini/martini.py:344-362).  mg_tune times the contraction of the
+ * caller's own problem under every candidate shape and caches the fastest
+ * for the problem's class: form, kernel table, spectral model, number of
+ * cubes, widest band, particle count (octave) and mean (tile, particle)
+ * pairs per tile (half octave, from max_pairs).  mg_insert* then use the
+ * cached shape of their class (the default when none is cached).  The cache
+ * is per process and guarded by a mutex; it holds the only mutable
+ * library-wide state besides per-device attribute caches.
+ */
+typedef struct mg_tuning {
+  int32_t kc;            /* particles per tensor-core stage: 0 = the form's default
+                            (64 for pairs, 32 for bf16x6), or 32 (pair forms) */
+  int32_t items_per_sm;  /* work items per SM (split-K granularity), 1..24; 0 = 24 */
+  int32_t cost_order;    /* 1: work queue ordered by estimated cost, largest first;
+                            0: segment (tile) order */
+  int32_t reserved;
+} mg_tuning;
+
+/* The default launch shape: kc 0, 24 items per SM, cost order. */
+void mg_tuning_default(mg_tuning* out);
+
+/* Candidate shapes mg_tune times for a form: up to cap into out; returns
+ * how many there are. */
+int mg_tuning_candidates(int32_t form, mg_tuning* out, int32_t cap);
+
+/*
+ * Autotune: for every candidate shape bin the problem (batch) and time its
+ * contraction stage `reps` times with CUDA events on the stream; cache the
+ * fastest (smallest median) for the problem's class and return it in *best
+ * (and its time in *best_ms, if not NULL).  Same workspace contract as
+ * mg_insert.  SYNCHRONISES the stream.  Runs with accumulate off, so it
+ * OVERWRITES the cubes: call it before the insertion whose result is kept.
+ */
+int mg_tune_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                    size_t workspace_bytes, int64_t max_pairs, int64_t max_partial_items,
+                    int32_t reps, void* stream, mg_tuning* best, float* best_ms);
+int mg_tune(const mg_problem* p, void* workspace, size_t workspace_bytes, int64_t max_pairs,
+            int64_t max_partial_items, int32_t reps, void* stream, mg_tuning* best,
+            float* best_ms);
+
+/* The cached shape of this problem's class: 1 and *out when cached, 0 and
+ * the default when not.  Host only (no GPU access). */
+int mg_tuning_lookup(const mg_problem* probs, int32_t nprob, int64_t max_pairs, mg_tuning* out);
+
+/* Cache a shape for this problem's class (e.g. one tuned in an earlier run).
+ * Host only.  Returns MG_ERR_INVALID_ARGUMENT for a shape the form cannot
+ * run. */
+int mg_tuning_store(const mg_problem* probs, int32_t nprob, int64_t max_pairs,
+                    const mg_tuning* t);
+
+/* Forget every cached shape. */
+void mg_tuning_reset(void);
+
+/*
  * GPU set-up: what Martini.__init__ does on the host before the insertion,
  * in FP64 on the GPU.  Per particle: sky position, distance and line-of-sight
  * velocity (martini/sources/sph_source.py:265-326), TAN projection to pixel

@@ -44,7 +44,9 @@ EXPORTS = ("mg_version", "mg_last_error", "mg_workspace_size", "mg_plan", "mg_in
            "mg_insert_stages", "mg_check", "mg_spectra", "mg_flux", "mg_insert_noalloc",
            "mg_workspace_size_batched", "mg_plan_batched", "mg_insert_batched",
            "mg_insert_stages_batched", "mg_setup_workspace_size", "mg_setup",
-           "mg_global_profile_workspace_size", "mg_global_profile", "mg_convolve_beam")
+           "mg_global_profile_workspace_size", "mg_global_profile", "mg_convolve_beam",
+           "mg_tuning_default", "mg_tuning_candidates", "mg_tune", "mg_tune_batched",
+           "mg_tuning_lookup", "mg_tuning_store", "mg_tuning_reset")
 
 MG_NOALLOC_SCRATCH_BYTES = 128 << 20
 
@@ -108,6 +110,16 @@ MG_PRUNE_MASS = 4
 MG_PRUNE_ALL = 7
 
 
+class Tuning(C.Structure):
+    """mg_tuning: the launch shape of an insertion (its autotuner's choice)."""
+    _fields_ = [("kc", C.c_int32), ("items_per_sm", C.c_int32), ("cost_order", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"kc": int(self.kc), "items_per_sm": int(self.items_per_sm),
+                "cost_order": int(self.cost_order)}
+
+
 class PlanInfo(C.Structure):
     _fields_ = [("n_pairs", C.c_int64), ("n_items", C.c_int64), ("n_partial_items", C.c_int64),
                 ("n_tiles", C.c_int64), ("workspace_bytes", C.c_size_t)]
@@ -166,10 +178,22 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.mg_spectra.argtypes = [P(Problem), C.c_void_p, C.c_void_p]
     lib.mg_flux.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                             C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.mg_tuning_default.argtypes = [P(Tuning)]
+    lib.mg_tuning_default.restype = None
+    lib.mg_tuning_candidates.argtypes = [C.c_int32, P(Tuning), C.c_int32]
+    lib.mg_tune.argtypes = [P(Problem), C.c_void_p, C.c_size_t, C.c_int64, C.c_int64, C.c_int32,
+                            C.c_void_p, P(Tuning), P(C.c_float)]
+    lib.mg_tune_batched.argtypes = [P(Problem), C.c_int32, C.c_void_p, C.c_size_t, C.c_int64,
+                                    C.c_int64, C.c_int32, C.c_void_p, P(Tuning), P(C.c_float)]
+    lib.mg_tuning_lookup.argtypes = [P(Problem), C.c_int32, C.c_int64, P(Tuning)]
+    lib.mg_tuning_store.argtypes = [P(Problem), C.c_int32, C.c_int64, P(Tuning)]
+    lib.mg_tuning_reset.argtypes = []
+    lib.mg_tuning_reset.restype = None
     for f in ("mg_workspace_size", "mg_plan", "mg_insert", "mg_insert_stages", "mg_check",
               "mg_spectra", "mg_flux", "mg_insert_noalloc", "mg_workspace_size_batched",
               "mg_plan_batched", "mg_insert_batched", "mg_insert_stages_batched", "mg_setup",
-              "mg_global_profile", "mg_convolve_beam"):
+              "mg_global_profile", "mg_convolve_beam", "mg_tuning_candidates", "mg_tune",
+              "mg_tune_batched", "mg_tuning_lookup", "mg_tuning_store"):
         getattr(lib, f).restype = C.c_int
     _lib = lib
     return lib

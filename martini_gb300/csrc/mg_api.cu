@@ -1,7 +1,10 @@
 // C ABI of the martini_gb300 library (declared in include/martini_gb300.h).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -326,7 +329,8 @@ int make_batch(const mg_problem* probs, int nprob, Batch* b, bool shape_only = f
   g.nedge = nedge;
   g.nrows = (int)nrows;
   g.nfpart = nfpart;
-  g.cbits = channel_bits(g.max_nc);
+  // sort-key bits below the segment: a kernel-class bit above the channel
+  g.cbits = channel_bits(g.max_nc) + 1;
   return MG_OK;
 }
 
@@ -408,14 +412,59 @@ int mg_workspace_size(const mg_problem* p, int64_t max_pairs, int64_t max_partia
 
 namespace {
 
+// ---------------------------------------------------------------------------
+// Launch shapes: validation, the per-class cache and the problem class key
+// ---------------------------------------------------------------------------
+
+bool shape_ok(int form, const mg_tuning& t) {
+  if (t.items_per_sm < 0 || t.items_per_sm > ITEMS_PER_SM) return false;
+  if (t.cost_order != 0 && t.cost_order != 1) return false;
+  if (t.kc == 0) return true;
+  if (form == MG_FORM_FP32) return false;
+  if (form == MG_FORM_BF16X6) return t.kc == 32;
+  return t.kc == 32 || t.kc == 64;
+}
+
+// The launch shape into the batch constants.  A plan (no particle list)
+// bins with the default items per SM: its split-K bound then holds for
+// every shape, whose items per SM never exceed the default.
+void apply_shape(const mg_tuning* t, bool scatter, Geo* g) {
+  mg_tuning d;
+  mg_tuning_default(&d);
+  const mg_tuning& u = (t && shape_ok(g->form, *t)) ? *t : d;
+  g->kc = u.kc;
+  g->items_per_sm = (scatter && u.items_per_sm > 0) ? u.items_per_sm : ITEMS_PER_SM;
+  g->cost_order = u.cost_order;
+}
+
+std::mutex g_tune_mu;
+std::map<std::string, mg_tuning> g_tune_cache;
+
+int floor_log2(double v) { return v >= 1.0 ? (int)std::floor(std::log2(v)) : -1; }
+
+// Problem class: form, kernel table, spectral model, cubes (octave), widest
+// band, particles (octave), pairs per tile (half octave).
+std::string class_key(const Batch& b, long long max_pairs) {
+  const Geo& g = b.g;
+  std::string k = "f" + std::to_string(g.form) + " m" + std::to_string(g.spectral_model);
+  for (int i = 0; i < g.n_kernels; ++i)
+    k += " k" + std::to_string(g.ks[i].type) + ":" + std::to_string((int)(g.ks[i].truncate * 16));
+  const double ppt = g.ntiles > 0 ? (double)max_pairs / (double)g.ntiles : 0.0;
+  k += " g" + std::to_string(floor_log2((double)g.ngal)) + " c" + std::to_string(g.max_nc) +
+       " n" + std::to_string(floor_log2((double)g.n + 1.0)) + " t" +
+       std::to_string((int)std::floor(2.0 * std::log2(ppt + 1.0)));
+  return k;
+}
+
 // The stages of an insertion (MG_STAGE_* bits; `scatter` adds the particle
 // list to the binning stage); all asynchronous on stream s.
 int run(const mg_problem* probs, int nprob, void* ws, size_t bytes, cudaStream_t s,
         long long cap_pairs, long long cap_partial, int stages, bool scatter, Ws* wout,
-        Batch* bout) {
+        Batch* bout, const mg_tuning* shape) {
   Batch& b = *bout;
   int rc = make_batch(probs, nprob, &b);
   if (rc) return rc;
+  apply_shape(shape, scatter, &b.g);
   const Geo& g = b.g;
   if (cap_pairs < 0 || cap_partial < 0) return fail(MG_ERR_INVALID_ARGUMENT, "negative capacity");
   Ws w;
@@ -470,7 +519,8 @@ int mg_plan_batched(const mg_problem* probs, int32_t nprob, void* workspace,
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   Ws w{};
   Batch b;
-  int rc = run(probs, nprob, workspace, workspace_bytes, s, 0, 0, MG_STAGE_BIN, false, &w, &b);
+  int rc = run(probs, nprob, workspace, workspace_bytes, s, 0, 0, MG_STAGE_BIN, false, &w, &b,
+               nullptr);
   if (rc) return rc;
   WsHeader h;
   cudaError_t e = cudaMemcpyAsync(&h, w.hdr, sizeof(h), cudaMemcpyDeviceToHost, s);
@@ -501,8 +551,11 @@ int mg_insert_stages_batched(const mg_problem* probs, int32_t nprob, void* works
   if (stages & ~MG_STAGE_ALL) return fail(MG_ERR_INVALID_ARGUMENT, "unknown stage bits");
   Ws w;
   Batch b;
+  // the launch shape cached for this problem's class, if any
+  mg_tuning shape;
+  mg_tuning_lookup(probs, nprob, max_pairs, &shape);
   return run(probs, nprob, workspace, workspace_bytes, static_cast<cudaStream_t>(stream),
-             max_pairs, max_partial_items, stages, true, &w, &b);
+             max_pairs, max_partial_items, stages, true, &w, &b, &shape);
 }
 
 int mg_insert_batched(const mg_problem* probs, int32_t nprob, void* workspace,
@@ -613,3 +666,139 @@ extern "C" int mg_spectra(const mg_problem* p, float* out, void* stream) {
   if (e != cudaSuccess) return cuda_fail(e, "mg_spectra launch");
   return MG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Launch-shape autotuner (declared in include/martini_gb300.h)
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+void mg_tuning_default(mg_tuning* out) {
+  if (!out) return;
+  out->kc = 0;
+  out->items_per_sm = ITEMS_PER_SM;
+  out->cost_order = 1;
+  out->reserved = 0;
+}
+
+int mg_tuning_candidates(int32_t form, mg_tuning* out, int32_t cap) {
+  std::vector<mg_tuning> c;
+  const bool pairs = form == MG_FORM_BF16X3 || form == MG_FORM_F16X3;
+  const int kcs[2] = {0, 32};
+  const int ipss[2] = {ITEMS_PER_SM, ITEMS_PER_SM / 2};
+  for (int kc : kcs) {
+    if (kc && !pairs) continue;
+    for (int ips : ipss)
+      for (int order = 1; order >= 0; --order) {
+        mg_tuning t;
+        t.kc = kc;
+        t.items_per_sm = ips;
+        t.cost_order = order;
+        t.reserved = 0;
+        c.push_back(t);
+      }
+  }
+  for (int i = 0; out && i < cap && i < (int)c.size(); ++i) out[i] = c[i];
+  return (int)c.size();
+}
+
+int mg_tuning_lookup(const mg_problem* probs, int32_t nprob, int64_t max_pairs, mg_tuning* out) {
+  mg_tuning_default(out);
+  Batch b;
+  if (make_batch(probs, nprob, &b, true)) return 0;
+  const std::string key = class_key(b, max_pairs);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const auto it = g_tune_cache.find(key);
+  if (it == g_tune_cache.end()) return 0;
+  if (out) *out = it->second;
+  return 1;
+}
+
+int mg_tuning_store(const mg_problem* probs, int32_t nprob, int64_t max_pairs,
+                    const mg_tuning* t) {
+  if (!t) return fail(MG_ERR_INVALID_ARGUMENT, "null tuning");
+  Batch b;
+  int rc = make_batch(probs, nprob, &b, true);
+  if (rc) return rc;
+  if (!shape_ok(b.g.form, *t))
+    return fail(MG_ERR_INVALID_ARGUMENT, "launch shape not supported by this form");
+  const std::string key = class_key(b, max_pairs);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache[key] = *t;
+  return MG_OK;
+}
+
+void mg_tuning_reset(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache.clear();
+}
+
+int mg_tune_batched(const mg_problem* probs, int32_t nprob, void* workspace,
+                    size_t workspace_bytes, int64_t max_pairs, int64_t max_partial_items,
+                    int32_t reps, void* stream, mg_tuning* best, float* best_ms) {
+  if (!probs || nprob < 1 || !best) return fail(MG_ERR_INVALID_ARGUMENT, "null argument");
+  if (reps < 1) reps = 1;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the tuning runs overwrite the cubes: accumulate off
+  std::vector<mg_problem> pv(probs, probs + nprob);
+  for (mg_problem& p : pv) p.accumulate = 0;
+  mg_tuning cand[16];
+  const int nc = std::min(16, mg_tuning_candidates(pv[0].form, cand, 16));
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return cuda_fail(cudaGetLastError(), "mg_tune");
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_fail(cudaGetLastError(), "mg_tune");
+  }
+  int rc = MG_OK;
+  float best_t = 0.f;
+  int best_i = -1;
+  for (int c = 0; c < nc && rc == MG_OK; ++c) {
+    Ws w;
+    Batch b;
+    rc = run(pv.data(), nprob, workspace, workspace_bytes, s, max_pairs, max_partial_items,
+             MG_STAGE_BIN | MG_STAGE_SPEC, true, &w, &b, &cand[c]);
+    if (rc) break;
+    rc = mg_check(workspace, stream);
+    if (rc) break;
+    std::vector<float> ms;
+    for (int r = 0; r < reps && rc == MG_OK; ++r) {
+      cudaEventRecord(e0, s);
+      rc = run(pv.data(), nprob, workspace, workspace_bytes, s, max_pairs, max_partial_items,
+               MG_STAGE_CONTRACT, true, &w, &b, &cand[c]);
+      cudaEventRecord(e1, s);
+      if (rc) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = cuda_fail(cudaGetLastError(), "mg_tune timing");
+        break;
+      }
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms.push_back(t);
+    }
+    if (rc) break;
+    rc = mg_check(workspace, stream);
+    if (rc) break;
+    std::sort(ms.begin(), ms.end());
+    const float med = ms[ms.size() / 2];
+    if (best_i < 0 || med < best_t) {
+      best_t = med;
+      best_i = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  *best = cand[best_i];
+  if (best_ms) *best_ms = best_t;
+  return mg_tuning_store(probs, nprob, max_pairs, best);
+}
+
+int mg_tune(const mg_problem* p, void* workspace, size_t workspace_bytes, int64_t max_pairs,
+            int64_t max_partial_items, int32_t reps, void* stream, mg_tuning* best,
+            float* best_ms) {
+  return mg_tune_batched(p, 1, workspace, workspace_bytes, max_pairs, max_partial_items, reps,
+                         stream, best, best_ms);
+}
+
+}  // extern "C"

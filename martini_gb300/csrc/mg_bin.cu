@@ -144,6 +144,11 @@ __global__ void __launch_bounds__(PREP_THREADS) k_prep(Geo g, Ws w) {
           const bool lo_in = rec.ilo == 0 || xf32 - (float)(rec.ilo - 1) >= reach;
           const bool hi_in = rec.ihi == G.nx - 1 || (float)(rec.ihi + 1) - xf32 >= reach;
           if (lo_in && hi_in) rec.flags |= PREC_ROWS_COVER;
+          const float yf32 = (float)y;
+          const float reach_y = h * (1.f + 0x1p-18f) + 1e-6f * (fabsf(yf32) + 1.f);
+          const bool lo_jn = rec.jlo == 0 || yf32 - (float)(rec.jlo - 1) >= reach_y;
+          const bool hi_jn = rec.jhi == G.ny - 1 || (float)(rec.jhi + 1) - yf32 >= reach_y;
+          if (lo_jn && hi_jn) rec.flags |= PREC_COLS_COVER;
         }
         if (g.spectral_model == MG_SPECTRUM_TABLE) {
           rec.clo = 0;
@@ -332,7 +337,7 @@ __global__ void k_diff_prefix(Geo g, Ws w, int smem_cap) {
 __global__ void k_plan_finish(Geo g, Ws w, int num_sms) {
   __shared__ long long red[256];
   const long long total = w.hdr->n_pairs;
-  const int kch = item_particles(total, num_sms);
+  const int kch = item_particles(total, num_sms, g.items_per_sm);
   long long sb = 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.ntiles; t += gridDim.x * blockDim.x) {
     const long long cnt = w.tile_off[t + 1] - w.tile_off[t];
@@ -371,7 +376,11 @@ __device__ __forceinline__ int div_exact(int a, int b, float rb) {
   return q;
 }
 
-// Pairs in particle order: key = global segment << cbits | clo (one pair per
+// Pairs in particle order: key = global segment << cbits | class << (cbits -
+// 1) | clo, class = 1 for the Gaussian and cubic-spline kernels (their
+// particles then form stages of their own, after the table and Dirac
+// kernels' in each segment; the tensor-core producers take such stages on a
+// separate path) (one pair per
 // tile and channel block the particle's line meets), value = particle.  A
 // warp takes 32 particles, whose pairs are one contiguous range of the
 // output (pair_off is the exclusive scan of the counts); each lane writes
@@ -391,6 +400,7 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
     long long o = 0x7fffffffffffffffll;  // lanes past the end never match
     int np = 0, tx0 = 0, ty0 = 0, nty_span = 1, cb0 = 0, nb = 1, clo = 0, seg0 = 0, nty = 1,
         ncb = 1;
+    unsigned cls = 0u;
     if (P < g.n) {
       o = w.pair_off[P];
       np = w.npairs[P];
@@ -403,6 +413,8 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
         cb0 = G.ncb > 1 ? rec.clo / G.width : 0;
         nb = G.ncb > 1 ? rec.chi / G.width - cb0 + 1 : 1;
         clo = rec.clo;
+        const int kt = g.ks[rec.kslot].type;
+        cls = (kt == MG_KERNEL_GAUSSIAN || kt == MG_KERNEL_CUBIC_SPLINE) ? 1u : 0u;
         seg0 = G.seg0;
         nty = G.nty;
         ncb = G.ncb;
@@ -428,6 +440,7 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
       const int scb0 = __shfl_sync(0xffffffffu, cb0, src);
       const int snb = __shfl_sync(0xffffffffu, nb, src);
       const int sclo = __shfl_sync(0xffffffffu, clo, src);
+      const unsigned scls = __shfl_sync(0xffffffffu, cls, src);
       const int sseg0 = __shfl_sync(0xffffffffu, seg0, src);
       const int snty = __shfl_sync(0xffffffffu, nty, src);
       const int sncb = __shfl_sync(0xffffffffu, ncb, src);
@@ -441,7 +454,7 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
         const int a = div_exact(t, sspan, __frcp_rn((float)sspan));
         const int tx = stx0 + a, ty = sty0 + (t - a * sspan);
         const unsigned sg = (unsigned)(sseg0 + (tx * snty + ty) * sncb + cb);
-        keys[f] = (sg << g.cbits) | (unsigned)sclo;
+        keys[f] = (sg << g.cbits) | (scls << (g.cbits - 1)) | (unsigned)sclo;
         vals[f] = (int)(base + src);
       }
     }
@@ -509,7 +522,8 @@ __global__ void k_item_keys(Geo g, Ws w) {
       const double lc = (double)(left < kch ? left : kch);
       double q = lc * (2.0 * TILE_PX + (double)width) / cmax * 65535.0 + 0.5;
       if (q > 65535.0) q = 65535.0;
-      w.item_key[base + k] = 65535u - (unsigned)q;
+      // all keys equal: the stable sort keeps segment order
+      w.item_key[base + k] = g.cost_order ? 65535u - (unsigned)q : 0u;
       w.item_order[base + k] = (int)(base + k);
     }
   }

@@ -19,14 +19,17 @@ constexpr int TILE_J = 16;   // pixels along axis 1 (Dec index)
 constexpr int TILE_PX = TILE_I * TILE_J;
 constexpr int CBLK = 64;     // channels per FP32 work item
 constexpr int KCH_MIN = 2048;     // fewest particles per work item (split-K granularity)
-constexpr int ITEMS_PER_SM = 24;  // target work items per SM when the pairs allow
+constexpr int ITEMS_PER_SM = 24;  // default target work items per SM when the pairs allow
 
 // Particles per work item for a launch with `total_pairs` (tile, particle)
-// pairs: about ITEMS_PER_SM items per SM, a multiple of 64, at least
-// KCH_MIN.  Small problems keep fine items for load balance; large ones get
-// items long enough that split-K partial tiles stay few.
-__host__ __device__ inline int item_particles(long long total_pairs, int num_sms) {
-  const long long per = (long long)(num_sms > 0 ? num_sms : 1) * ITEMS_PER_SM;
+// pairs: about `items_per_sm` items per SM (1 .. ITEMS_PER_SM; the plan's
+// split-K bound holds for every value up to the default), a multiple of 64,
+// at least KCH_MIN.  Small problems keep fine items for load balance; large
+// ones get items long enough that split-K partial tiles stay few.
+__host__ __device__ inline int item_particles(long long total_pairs, int num_sms,
+                                              int items_per_sm = ITEMS_PER_SM) {
+  if (items_per_sm < 1 || items_per_sm > ITEMS_PER_SM) items_per_sm = ITEMS_PER_SM;
+  const long long per = (long long)(num_sms > 0 ? num_sms : 1) * items_per_sm;
   long long t = (total_pairs + per - 1) / per;
   t = (t + 63) / 64 * 64;
   if (t < KCH_MIN) t = KCH_MIN;
@@ -54,6 +57,8 @@ struct PRec {
 // the FP32 profile argument of any other row is past the support): a radial
 // table kernel needs no per-row box test.
 constexpr int PREC_ROWS_COVER = 1;
+// The same for the footprint's columns [jlo, jhi] (axis 1).
+constexpr int PREC_COLS_COVER = 2;
 
 struct KSpec {
   int type;
@@ -117,7 +122,8 @@ struct Geo {
   int nseg;           // segments of all cubes
   int max_width;      // widest channel block (partial slots hold TILE_PX x max_width)
   int max_nc;
-  int cbits;          // channel bits of the sort key (widest band)
+  int cbits;          // key bits below the segment: a kernel-class bit, then the channel
+                      // bits of the widest band
   int nrows;          // flux rows of all cubes
   int max_diff;       // largest difference array of one cube
   long long n;        // particles of all cubes
@@ -125,6 +131,12 @@ struct Geo {
   long long nedge;    // channel edges of all cubes
   long long nfpart;   // FP64 flux partials of all cubes
   KSpec ks[MG_MAX_KERNELS];
+  // launch shape (mg_tuning): particles per tensor-core stage (0: the
+  // form's default), work items per SM, cost-ordered work queue
+  int kc;
+  int items_per_sm;
+  int cost_order;
+  int pad_tuning;
 };
 
 // Cube of a batch-wide index: the largest k < ngal with keys[k] <= v (cubes
@@ -187,7 +199,7 @@ struct Ws {
   float* ehi;            // [nedge] edges, double-float high part
   float* elo;            // [nedge] low part
   float* inv_w;          // [nedge] 1 / |channel width| (channel c of a cube at edge0 + c)
-  unsigned* keys;        // [cap_pairs] sorted keys: segment << cbits | clo
+  unsigned* keys;        // [cap_pairs] sorted keys: segment << cbits | class | clo
   int* list;             // [cap_pairs] particle ids in sorted order
   unsigned* keys_tmp;    // [cap_pairs] radix-sort second buffer
   int* list_tmp;         // [cap_pairs]

@@ -1,9 +1,10 @@
 // Device-wide exclusive scan and stable LSD radix sort of (key, value) pairs.
 //
 // Used by the footprint binning: (tile, particle) pairs are emitted in
-// particle order and sorted by key = tile << cbits | first channel of the
-// particle's spectral support.  The sort is stable, so the order within a
-// tile and channel is particle order and the binning is deterministic.
+// particle order and sorted by key = segment << cbits | kernel class | first
+// channel of the particle's spectral support.  The sort is stable, so the
+// order within a segment, class and channel is particle order and the
+// binning is deterministic.
 #include "mg_internal.cuh"
 
 namespace mg {

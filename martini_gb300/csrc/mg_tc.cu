@@ -58,21 +58,24 @@ constexpr int SPLIT_BF16_2 = 1;
 constexpr int SPLIT_BF16_3 = 2;
 __host__ __device__ constexpr int split_parts(int split) { return split == SPLIT_BF16_3 ? 3 : 2; }
 __host__ __device__ constexpr bool split_bf16(int split) { return split != SPLIT_F16_2; }
-// particles per stage: 64 for pairs, 32 for three pieces (the same bytes)
+// default particles per stage: 64 for pairs, 32 for three pieces (the same
+// bytes); the pair forms also run with 32 (a launch-shape choice)
 __host__ __device__ constexpr int split_kc(int split) { return split == SPLIT_BF16_3 ? 32 : 64; }
 
 // Shared memory at the widest band: two stages of A and B pieces plus the
 // static arrays must fit in the 227 KB of a CTA.
-constexpr size_t tc_stage_bytes(int split, int nw) {
-  return (size_t)split_parts(split) * (split_kc(split) / 16) * (4096 + 32 * (size_t)nw);
+constexpr size_t tc_stage_bytes(int split, int kc, int nw) {
+  return (size_t)split_parts(split) * (kc / 16) * (4096 + 32 * (size_t)nw);
 }
 constexpr size_t tc_static_bytes(int kc) {
   return (KT_SMEM_CELLS + 257) * 16 + 2 * kc * (sizeof(PRec) + sizeof(int) + sizeof(long long)) +
          4096;
 }
-static_assert(2 * tc_stage_bytes(SPLIT_F16_2, TC_MASTER_COL) + tc_static_bytes(64) <= 227 * 1024,
+static_assert(2 * tc_stage_bytes(SPLIT_F16_2, 64, TC_MASTER_COL) + tc_static_bytes(64) <=
+                  227 * 1024,
               "tensor-core kernel shared memory (pairs)");
-static_assert(2 * tc_stage_bytes(SPLIT_BF16_3, TC_MASTER_COL) + tc_static_bytes(32) <= 227 * 1024,
+static_assert(2 * tc_stage_bytes(SPLIT_BF16_3, 32, TC_MASTER_COL) + tc_static_bytes(32) <=
+                  227 * 1024,
               "tensor-core kernel shared memory (three pieces)");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -191,6 +194,19 @@ __device__ __forceinline__ void tmem_st32_zero(unsigned taddr) {
       : "memory");
 }
 
+__device__ __forceinline__ void tmem_st32(unsigned taddr, const unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31, %32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
+      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
+      "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
@@ -230,24 +246,6 @@ __device__ __forceinline__ void split2(float v, unsigned short& hi, unsigned sho
     hi = __half_as_ushort(h);
     lo = __half_as_ushort(__float2half_rn(v - __half2float(h)));
   }
-}
-
-// Spectrum of one channel for the tensor-core producers (GAUSSIAN: the
-// erf difference across the channel, with erfc in the tails so that the
-// far wings of many lines do not accumulate cancellation error; DIRAC; TABLE).
-__device__ __forceinline__ float tc_spectrum(const PRec& r, int model, int c, int dec,
-                                             const float* ehi, const float* elo,
-                                             const float* inv_w, const float* spectra, int pid,
-                                             int nc) {
-  if (c < r.clo || c > r.chi) return 0.f;
-  if (model == MG_SPECTRUM_TABLE) return spectra[(long long)pid * nc + c];
-  const float iw = inv_w[c];
-  if (model == MG_SPECTRUM_DIRAC) return r.amp * iw;
-  const int e0 = dec ? c + 1 : c;  // lower edge
-  const int e1 = dec ? c : c + 1;  // upper edge
-  const float a = ((ehi[e0] - r.vhi) + (elo[e0] - r.vlo)) * r.inv_s;
-  const float b = ((ehi[e1] - r.vhi) + (elo[e1] - r.vlo)) * r.inv_s;
-  return r.amp * half_erf_diff(a, b) * iw;
 }
 
 struct ItemTC {
@@ -404,156 +402,6 @@ __device__ __forceinline__ float spec_scale(const GalState& gs, int model) {
   return sb > 0.f ? exp2f(14.f - ceilf(log2f(sb))) : 1.f;
 }
 
-// GaussianKernel pixel integral (sph_kernels.py:994-1044) at the four
-// pixels of a lane,
-//   W = 0.25 erf(zmax / sqrt 2) (erf(x1) - erf(x0)) (erf(y1) - erf(y0)) / norm,
-// zmax = sqrt(truncate^2 - q^2) (0 past the truncation), q = dr / (h sigma).
-// The row factors of the tile's 8 rows come from lanes 0-7 and the column
-// factors of its 16 columns from lanes 8-23 (two erff each, shared by
-// shuffles); the truncation factor comes from its table in zmax (cubic cells,
-// ~6e-8).  Called by all 32 lanes.
-__device__ __forceinline__ void weights4_gauss(const PRec& r, const KSpec& kk, unsigned gtab_s32,
-                                               int ib, int j, int lane, float sw,
-                                               float (&w)[4]) {
-  const float inv_hs = 1.f / (r.h * 0.42466090014400953f);  // 1 / (h sigma_FWHM)
-  const float sc = inv_hs * 0.70710678118654752f;            // 1 / (h sqrt(2) sigma)
-  const int i0 = ib - (lane >> 4), j0 = j - (lane & 15);
-  const float d = lane < 8 ? (float)(r.xi - (i0 + lane)) + r.xf
-                           : (float)(r.yi - (j0 + ((lane - 8) & 15))) + r.yf;
-  const float e = erff((d + 0.5f) * sc) - erff((d - 0.5f) * sc);
-  const float ey = __shfl_sync(0xffffffffu, e, 8 + (lane & 15));
-  float ex[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) ex[k] = __shfl_sync(0xffffffffu, e, (lane >> 4) + 2 * k);
-  if (j < r.jlo || j > r.jhi) return;
-  const float dy = (float)(r.yi - j) + r.yf;
-  const float dy2 = dy * dy;
-  const float ihs2 = inv_hs * inv_hs;
-  const float t2 = kk.truncate * kk.truncate;
-  const float c = 0.25f / kk.gnorm * ey * sw;
-  const float dx0 = (float)(r.xi - ib) + r.xf;
-  const unsigned base32 = gtab_s32 - (0x4B000000u << 4);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int i = ib + 2 * k;
-    const float dxk = dx0 - (float)(2 * k);
-    const float z2 = fmaxf(fmaf(-fmaf(dxk, dxk, dy2), ihs2, t2), 0.f);  // truncate^2 - q^2
-    const float u = fminf(sqrt_approx(z2) * GT_CELLS_PER_UNIT, (float)GT_NCELL);
-    float t;
-    const float4 cf = kt_cell_smem(base32, u, t);
-    const float T = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
-    w[k] = (i >= r.ilo && i <= r.ihi) ? T * ex[k] * c : 0.f;
-  }
-}
-
-// W of one particle at the four pixels of a lane: rows ib + 2 k, column j.
-// ktab_s32 is the shared address of the launch's radial table (type
-// ktab_type, copied from its first cell); other radial types read kt_coef.
-__device__ __forceinline__ void weights4(const PRec& r, bool valid, const KSpec* ks,
-                                         const float4* ktab, unsigned ktab_s32, int ktab_type,
-                                         unsigned gtab_s32, int ib, int j, int lane, float sw,
-                                         float (&w)[4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) w[k] = 0.f;
-  if (!valid) return;  // warp-uniform
-  const KSpec kk = ks[r.kslot];
-  if (kk.type == MG_KERNEL_GAUSSIAN) {  // warp-uniform; every lane takes part
-    weights4_gauss(r, kk, gtab_s32, ib, j, lane, sw, w);
-    return;
-  }
-  if (j < r.jlo || j > r.jhi) return;
-  const float dy = (float)(r.yi - j) + r.yf;
-  if (kk.type <= MG_KERNEL_QUARTIC_SPLINE && kk.type != MG_KERNEL_CUBIC_SPLINE) {
-    // cells in s = R^2: the cell coordinate u = s * cells per unit s is
-    // clamped onto the zero cell past the support, so no support test
-    const KTableInfo& inf = kt_info[kk.type];
-    const float k2 = r.inv_h2 * inf.reg[0].cells_per_unit;
-    const float ucap = (float)inf.reg[0].ncell;
-    const float scale = inf.scale * r.inv_h2 * sw;
-    const float dy2k = dy * dy * k2;
-    const float dx0 = (float)(r.xi - ib) + r.xf;
-    float u[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float dxk = dx0 - (float)(2 * k);
-      u[k] = fminf(fmaf(dxk * k2, dxk, dy2k), ucap);
-    }
-    if (!(r.flags & PREC_ROWS_COVER)) {  // rows outside the footprint box: zero cell
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int i = ib + 2 * k;
-        if (i < r.ilo || i > r.ihi) u[k] = ucap;
-      }
-    }
-    if (kk.type == ktab_type) {
-      const unsigned base32 = ktab_s32 - (0x4B000000u << 4);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        float t;
-        const float4 cf = kt_cell_smem(base32, u[k], t);
-        w[k] = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x) * scale;
-      }
-    } else {
-      const float4* tab = reinterpret_cast<const float4*>(kt_coef) + inf.reg[0].first;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        float t;
-        const int c = kt_floor(u[k], t);
-        const float4 cf = __ldg(tab + c);
-        w[k] = fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x) * scale;
-      }
-    }
-    return;
-  }
-  float dx[4];
-  bool in[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int i = ib + 2 * k;
-    in[k] = i >= r.ilo && i <= r.ihi;
-    dx[k] = (float)(r.xi - i) + r.xf;
-  }
-  if (kk.type == MG_KERNEL_DIRAC) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) w[k] = in[k] ? sw : 0.f;
-  } else {  // cubic spline: cells in R and A = sqrt(1 - R^2)
-    const KTableInfo& inf = kt_info[kk.type];
-    const float fac = 4.f * r.inv_h2;
-    const float scale = inf.scale * r.inv_h2 * sw;
-    const float dy2 = dy * dy;
-    const float4* tab = kk.type == ktab_type ? ktab : reinterpret_cast<const float4*>(kt_coef);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float f = kt_eval_cubic(inf, tab, fmaf(dx[k], dx[k], dy2) * fac);
-      w[k] = in[k] ? f * scale : 0.f;
-    }
-  }
-}
-
-// A = W for particles (q, q + 1): lane l covers pixels l + 32 k, k = 0..3,
-// which share the column j = j0 + (l & 15).
-template <int SPLIT>
-__device__ __forceinline__ void produce_w_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
-                                               const KSpec* ks, const float4* ktab,
-                                               unsigned ktab_s32, int ktab_type,
-                                               unsigned gtab_s32, int q, int i0, int j0, int lane,
-                                               float sw, unsigned char* a0, unsigned a_bytes) {
-  const int j = j0 + (lane & 15);
-  const int ib = i0 + (lane >> 4);
-  float w0[4], w1[4];
-  weights4(r0, v0, ks, ktab, ktab_s32, ktab_type, gtab_s32, ib, j, lane, sw, w0);
-  weights4(r1, v1, ks, ktab, ktab_s32, ktab_type, gtab_s32, ib, j, lane, sw, w1);
-  // element (pixel p, particle q): K step q / 16, K core q / 8 % 2, (q % 8) * 2
-  const unsigned qoff = (unsigned)(q >> 4) * 4096u + (unsigned)((q >> 3) & 1) * 128u +
-                        (unsigned)(q & 7) * 2u;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int p = lane + 32 * k;
-    const unsigned off = qoff + (unsigned)(p >> 3) * 256u + (unsigned)(p & 7) * 16u;
-    store_split<SPLIT>(w0[k], w1[k], a0, a_bytes, off);
-  }
-}
-
 // erfc(z) for z >= 0 by the Chebyshev-fitted form of Press, Teukolsky,
 // Vetterling & Flannery, Numerical Recipes (2nd ed., section 6.2, "erfcc"):
 // erfc(z) = t exp(-z^2 + P(t)), t = 1 / (1 + z / 2), fractional error below
@@ -588,77 +436,20 @@ __device__ __forceinline__ float half_diff_from_c(float ca, bool pa, float cb, b
   return (pa || !pb) ? both : fmaf(-0.5f, ca + cb, 1.f);
 }
 
-// Spectrum store value of channel c for a particle (0 outside its support).
-// A particle's spectrum-store row: channel clo first, n support channels (0
-// for a particle that contributes nothing, so every lookup gives 0).
-struct SpecRow {
-  const unsigned* row;
-  int clo;
-  unsigned n;
-};
-
-__device__ __forceinline__ SpecRow spec_row(const unsigned* spec, long long soff, const PRec& r,
-                                            bool v) {
-  SpecRow q;
-  q.row = spec + soff;
-  q.clo = r.clo;
-  q.n = (v && r.chi >= r.clo) ? (unsigned)(r.chi - r.clo + 1) : 0u;
-  return q;
-}
-
-// one unsigned compare: c below clo wraps past n
-__device__ __forceinline__ unsigned spec_at(const SpecRow& q, int c) {
-  const unsigned d = (unsigned)(c - q.clo);
-  return d < q.n ? __ldg(q.row + d) : 0u;
-}
-
-// B = S for particles (q, q + 1) over the window channels.  A Gaussian line
-// needs erfc at every window edge once: in step m lane l evaluates edge
-// 31 m + l and channel 31 m + l (l < 31) takes its upper index edge from
-// lane l + 1, so each step covers 31 channels with no repeated evaluation.
+// B = S for particles (q, q + 1) over the window channels, lines evaluated
+// here (no spectrum store).  A Gaussian line needs erfc at every window edge
+// once: in step m lane l evaluates edge 31 m + l and channel 31 m + l
+// (l < 31) takes its upper index edge from lane l + 1, so each step covers
+// 31 channels with no repeated evaluation.
 template <int SPLIT>
 __device__ __forceinline__ void produce_s_pair(const PRec& r0, const PRec& r1, bool v0, bool v1,
                                                int q, int w0, int nw, int nc, int dec, int model,
                                                const float* ehi, const float* elo,
                                                const float* inv_w, const float* spectra,
                                                int pid0, int pid1, int lane, float ss,
-                                               const unsigned* spec, long long soff0,
-                                               long long soff1, unsigned pf0, unsigned pf1,
-                                               unsigned pf2, unsigned pf3, unsigned char* b0,
-                                               unsigned b_bytes) {
+                                               unsigned char* b0, unsigned b_bytes) {
   const unsigned qoff = (unsigned)(q >> 4) * ((unsigned)nw * 32u) +
                         (unsigned)((q >> 3) & 1) * 128u + (unsigned)(q & 7) * 2u;
-  if (spec) {
-    // Gaussian lines read from the spectrum store, already scaled and split
-    // (hi | lo << 16 per value; the FP32 value for three pieces); the first
-    // 64 window channels were loaded before the weights
-    const SpecRow q0 = spec_row(spec, soff0, r0, v0), q1 = spec_row(spec, soff1, r1, v1);
-    for (int base = 0; base < nw; base += 32) {  // warp-uniform
-      const int n = base + lane;
-      const int c = w0 + n;
-      unsigned s0, s1;
-      if (base == 0) {
-        s0 = pf0;
-        s1 = pf1;
-      } else if (base == 32) {
-        s0 = pf2;
-        s1 = pf3;
-      } else {
-        s0 = spec_at(q0, c);
-        s1 = spec_at(q1, c);
-      }
-      if (n < nw) {
-        const unsigned off = qoff + (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
-        if constexpr (SPLIT == SPLIT_BF16_3) {
-          store_split<SPLIT>(__uint_as_float(s0), __uint_as_float(s1), b0, b_bytes, off);
-        } else {
-          *reinterpret_cast<unsigned*>(b0 + off) = __byte_perm(s0, s1, 0x5410);
-          *reinterpret_cast<unsigned*>(b0 + b_bytes + off) = __byte_perm(s0, s1, 0x7632);
-        }
-      }
-    }
-    return;
-  }
   const bool gauss = model == MG_SPECTRUM_GAUSSIAN;
   const int step = gauss ? 31 : 32;
   for (int base = 0; base < nw; base += step) {  // warp-uniform
@@ -804,6 +595,339 @@ __global__ void k_spec_eval(Geo g, Ws w) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Stage parameters and the operand producers.
+//
+// When a stage's records arrive, the record warps turn each particle into a
+// compact StagePar (tile-relative position, kernel constants, footprint box)
+// and SPar (its spectrum-store row).  The producers read these as warp-wide
+// broadcasts and write operand rows of 8 particles (16 bytes per piece), so
+// a quarter-warp stores 128 contiguous bytes: no shared-memory bank
+// conflicts.
+//
+// Weights: warp w takes particle group g8 = w % (KC / 8) (8 particles) and
+// pixel group pg = w / (KC / 8); lane l holds PXL = KC / 32 pixels,
+// m = 32 (pg PXL + k) + l, i.e. tile row 2 (pg PXL + k) + l / 16 and column
+// l % 16.  A particle whose footprint rows miss the warp's 2 PXL rows is
+// skipped by the whole warp (exact: the reference weighs only pixels in the
+// box).  Spectra: one task per (32-channel chunk of the stage window,
+// 8-particle group); lane l takes window channel 32 chunk + l.
+// ---------------------------------------------------------------------------
+
+constexpr int WK_NONE = 0;   // contributes nothing to this segment
+constexpr int WK_TAB = 1;    // radial kernel, s-cells in shared memory
+constexpr int WK_TABG = 2;   // radial kernel, s-cells in global memory
+constexpr int WK_CUBIC = 3;  // cubic spline (cells in R and sqrt(1 - R^2))
+constexpr int WK_GAUSS = 4;
+constexpr int WK_DIRAC = 5;
+constexpr int WK_COVER = 8;  // the box holds the support in rows and columns: no box test
+
+struct StagePar {
+  float dxr, xf;  // xi - i0 (exact), x - xi
+  float dyr, yf;  // yi - j0 (exact), y - yi
+  float k2;       // TAB/TABG: inv_h2 * cells per unit s; CUBIC: 4 inv_h2; GAUSS: 1 / (h sigma)
+  float scale;    // TAB/TABG/CUBIC: table scale * inv_h2 * sw; GAUSS: 0.25 / gnorm * sw;
+                  // DIRAC: sw
+  int kind;       // WK_* | WK_COVER, kernel slot << 8, kernel type << 12
+  int mask;       // footprint box within the tile: row bits 0-7, column bits 8-23 (all set
+                  // when the box holds the support: no test needed; none for WK_NONE)
+};
+static_assert(sizeof(StagePar) == 32, "two 16-byte broadcasts per particle");
+
+struct SPar {
+  long long soff;  // spectrum-store row of the particle (cp.async target)
+  int clo;         // first support channel
+  unsigned n;      // support channels in the row; 0: contributes nothing
+};
+
+// StagePar / SPar of one particle of a stage (valid: listed for this stage;
+// the record of an unused slot is empty).  Returns the WK_* kind.
+__device__ __forceinline__ int build_par(const PRec& r, bool valid, int i0, int j0, int cb0,
+                                         int cb1, const KSpec* ks, int ktab_type, float sw,
+                                         StagePar& P, SPar& S) {
+  valid = valid && r.ilo <= r.ihi && r.jlo <= r.jhi && r.chi >= cb0 && r.clo <= cb1;
+  const KSpec kk = ks[r.kslot];
+  const int t = kk.type;
+  int kind = WK_NONE;
+  float k2 = 0.f, scale = 0.f;
+  if (valid) {
+    if (t == MG_KERNEL_DIRAC) {
+      kind = WK_DIRAC;
+      scale = sw;
+    } else if (t == MG_KERNEL_GAUSSIAN) {
+      kind = WK_GAUSS;
+      k2 = 1.f / (r.h * 0.42466090014400953f);  // 1 / (h sigma_FWHM)
+      scale = 0.25f / kk.gnorm * sw;
+    } else {
+      const KTableInfo& inf = kt_info[t];
+      if (t == MG_KERNEL_CUBIC_SPLINE) {
+        kind = WK_CUBIC;
+        k2 = 4.f * r.inv_h2;
+      } else {
+        kind = t == ktab_type ? WK_TAB : WK_TABG;
+        k2 = r.inv_h2 * inf.reg[0].cells_per_unit;
+      }
+      scale = inf.scale * r.inv_h2 * sw;
+      if ((r.flags & PREC_ROWS_COVER) && (r.flags & PREC_COLS_COVER)) kind |= WK_COVER;
+    }
+  }
+  P.dxr = (float)(r.xi - i0);
+  P.xf = r.xf;
+  P.dyr = (float)(r.yi - j0);
+  P.yf = r.yf;
+  P.k2 = k2;
+  P.scale = scale;
+  P.kind = kind | (r.kslot << 8) | (t << 12);
+  // box rows / columns within the tile as bit masks
+  unsigned rows = 0u, cols = 0u;
+  if (kind != WK_NONE) {
+    const int a = max(r.ilo - i0, 0), b = min(r.ihi - i0, TILE_I - 1);
+    const int c = max(r.jlo - j0, 0), d = min(r.jhi - j0, TILE_J - 1);
+    if (a <= b) rows = ((2u << b) - 1u) & ~((1u << a) - 1u);
+    if (c <= d) cols = ((2u << d) - 1u) & ~((1u << c) - 1u);
+    if (kind & WK_COVER) {
+      // rows outside the box still need no test (the table's zero cell), but
+      // the warps whose rows miss the box skip it: keep the row bits
+      cols = 0xFFFFu;
+    }
+  }
+  P.mask = (int)(rows | cols << 8);
+  S.clo = r.clo;
+  S.n = (valid && r.chi >= r.clo) ? (unsigned)(r.chi - r.clo + 1) : 0u;
+  return kind & 7;
+}
+
+// The group flags of a stage's particles, one thread per particle (whole
+// warps; lanes 8 g .. 8 g + 7 hold group g of the warp): 1 when all eight
+// are WK_NONE, WK_TAB or WK_DIRAC.
+__device__ __forceinline__ void group_flags(int kind, int tid, int* flags) {
+  const bool simple = kind == WK_NONE || kind == WK_TAB || kind == WK_DIRAC;
+  const unsigned bal = __ballot_sync(0xffffffffu, simple);
+  const int lane = tid & 31;
+  if ((lane & 7) == 0) flags[tid >> 3] = ((bal >> lane) & 0xFFu) == 0xFFu;
+}
+
+__device__ __forceinline__ float horner3(const float4& cf, float t) {
+  return fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
+}
+
+// Weights of one stage particle at a lane's PXL pixels (tile rows il[k],
+// column jl).  Warp-uniform: every lane takes the same branch.
+template <int PXL>
+__device__ __forceinline__ void w_particle(const StagePar& P, const KSpec* ks, unsigned ktab_s32,
+                                           float ucap, int wr0, const int (&il)[PXL],
+                                           const float (&ilf)[PXL], int jl, float jlf, int lane,
+                                           float (&w)[PXL]) {
+#pragma unroll
+  for (int k = 0; k < PXL; ++k) w[k] = 0.f;
+  const int kind = P.kind & 7;
+  const unsigned rows = (unsigned)P.mask & 0xFFu;
+  // the warp's rows are wr0 .. wr0 + 2 PXL - 1
+  if (kind == WK_NONE || ((rows >> wr0) & ((1u << (2 * PXL)) - 1u)) == 0u) return;
+  const bool jin = ((unsigned)P.mask >> (8 + jl)) & 1u;
+  bool in[PXL];
+#pragma unroll
+  for (int k = 0; k < PXL; ++k) in[k] = jin && ((rows >> il[k]) & 1u);
+  const float dy = (P.dyr - jlf) + P.yf;
+  float dx[PXL];
+#pragma unroll
+  for (int k = 0; k < PXL; ++k) dx[k] = (P.dxr - ilf[k]) + P.xf;
+  if (kind == WK_TAB) {
+    // cells in s = R^2 in shared memory; u clamped onto the zero cell past
+    // the support, so a covered particle needs no box test
+    const float dy2k = dy * dy * P.k2;
+    const bool cover = (P.kind & WK_COVER) != 0;
+    const unsigned base32 = ktab_s32 - (0x4B000000u << 4);
+#pragma unroll
+    for (int k = 0; k < PXL; ++k) {
+      float u = fminf(fmaf(dx[k] * P.k2, dx[k], dy2k), ucap);
+      if (!cover && !in[k]) u = ucap;
+      float t;
+      const float4 cf = kt_cell_smem(base32, u, t);
+      w[k] = horner3(cf, t) * P.scale;
+    }
+    return;
+  }
+  if (kind == WK_GAUSS) {
+    // GaussianKernel pixel integral (sph_kernels.py:994-1044):
+    // 0.25 erf(zmax / sqrt 2) (erf(x1) - erf(x0)) (erf(y1) - erf(y0)) / norm.
+    // Column factors from lanes 0-15, the warp's row factors from lanes
+    // 16 .. 16 + 2 PXL - 1 (two erff each), shared by shuffles; the
+    // truncation factor from its cubic cells in zmax.
+    const float inv_hs = P.k2;
+    const float sc = inv_hs * 0.70710678118654752f;  // 1 / (h sqrt(2) sigma)
+    const float d = lane < 16 ? (P.dyr - (float)lane) + P.yf
+                              : (P.dxr - (float)(wr0 + ((lane - 16) & (2 * PXL - 1)))) + P.xf;
+    const float e = erff((d + 0.5f) * sc) - erff((d - 0.5f) * sc);
+    const float ey = __shfl_sync(0xffffffffu, e, jl);
+    const KSpec kk = ks[(P.kind >> 8) & 0xF];
+    const float t2 = kk.truncate * kk.truncate;
+    const float ihs2 = inv_hs * inv_hs;
+    const float dy2 = dy * dy;
+    const float c = ey * P.scale;
+    const float4* gt = reinterpret_cast<const float4*>(gt_coef);
+#pragma unroll
+    for (int k = 0; k < PXL; ++k) {
+      const float ex = __shfl_sync(0xffffffffu, e, 16 + (il[k] - wr0));
+      const float z2 = fmaxf(fmaf(-fmaf(dx[k], dx[k], dy2), ihs2, t2), 0.f);  // truncate^2 - q^2
+      const float u = fminf(sqrt_approx(z2) * GT_CELLS_PER_UNIT, (float)GT_NCELL);
+      float t;
+      const int cell = kt_floor(u, t);
+      const float T = horner3(__ldg(gt + cell), t);
+      w[k] = in[k] ? T * ex * c : 0.f;
+    }
+    return;
+  }
+  if (kind == WK_DIRAC) {
+#pragma unroll
+    for (int k = 0; k < PXL; ++k) w[k] = in[k] ? P.scale : 0.f;
+    return;
+  }
+  const int type = (P.kind >> 12) & 0xF;
+  const KTableInfo& inf = kt_info[type];
+  const bool cover = (P.kind & WK_COVER) != 0;
+  if (kind == WK_CUBIC) {
+    const float4* tab = reinterpret_cast<const float4*>(kt_coef);
+    const float dy2 = dy * dy;
+#pragma unroll
+    for (int k = 0; k < PXL; ++k) {
+      const float f = kt_eval_cubic(inf, tab, fmaf(dx[k], dx[k], dy2) * P.k2);
+      w[k] = (cover || in[k]) ? f * P.scale : 0.f;
+    }
+    return;
+  }
+  // WK_TABG: another radial kernel's s-cells from global memory
+  const float4* tab = reinterpret_cast<const float4*>(kt_coef) + inf.reg[0].first;
+  const float gcap = (float)inf.reg[0].ncell;
+  const float dy2k = dy * dy * P.k2;
+#pragma unroll
+  for (int k = 0; k < PXL; ++k) {
+    float u = fminf(fmaf(dx[k] * P.k2, dx[k], dy2k), gcap);
+    if (!cover && !in[k]) u = gcap;
+    float t;
+    const int cell = kt_floor(u, t);
+    w[k] = horner3(__ldg(tab + cell), t) * P.scale;
+  }
+}
+
+// Pieces of 8 consecutive particles' values (one core-matrix row), stored as
+// one 16-byte row per piece at byte offset off of each piece's tile.
+template <int SPLIT>
+__device__ __forceinline__ void store_row8(unsigned char* base, unsigned piece_bytes,
+                                           unsigned off, const float (&v)[8]) {
+  if constexpr (SPLIT == SPLIT_BF16_3) {
+    uint4 h, m, l;
+    split3_pair(v[0], v[1], h.x, m.x, l.x);
+    split3_pair(v[2], v[3], h.y, m.y, l.y);
+    split3_pair(v[4], v[5], h.z, m.z, l.z);
+    split3_pair(v[6], v[7], h.w, m.w, l.w);
+    *reinterpret_cast<uint4*>(base + off) = h;
+    *reinterpret_cast<uint4*>(base + piece_bytes + off) = m;
+    *reinterpret_cast<uint4*>(base + 2 * piece_bytes + off) = l;
+  } else {
+    uint4 h, l;
+    split_pair<split_bf16(SPLIT)>(v[0], v[1], h.x, l.x);
+    split_pair<split_bf16(SPLIT)>(v[2], v[3], h.y, l.y);
+    split_pair<split_bf16(SPLIT)>(v[4], v[5], h.z, l.z);
+    split_pair<split_bf16(SPLIT)>(v[6], v[7], h.w, l.w);
+    *reinterpret_cast<uint4*>(base + off) = h;
+    *reinterpret_cast<uint4*>(base + piece_bytes + off) = l;
+  }
+}
+
+// A = W of one 8-particle group over the warp's pixel group.  `simple`: every
+// particle of the group is WK_NONE, WK_TAB or WK_DIRAC, so the 8 x PXL
+// weights are one branch-free block of independent chains (NONE: empty
+// mask and zero scale, which the table's zero cell turns into 0; DIRAC: the
+// box test picks sw); otherwise each particle takes its kind's path.
+template <int SPLIT, int PXL>
+__device__ __forceinline__ void produce_w_task(const StagePar* par, bool simple, const KSpec* ks,
+                                               unsigned ktab_s32, float ucap, int g8, int pg,
+                                               int lane, unsigned char* a0, unsigned a_bytes) {
+  const int jl = lane & 15;
+  const float jlf = (float)jl;
+  const int wr0 = 2 * pg * PXL;
+  int il[PXL];
+  float ilf[PXL];
+#pragma unroll
+  for (int k = 0; k < PXL; ++k) {
+    il[k] = wr0 + 2 * k + (lane >> 4);
+    ilf[k] = (float)il[k];
+  }
+  float w[8][PXL];
+  if (simple) {
+    const unsigned base32 = ktab_s32 - (0x4B000000u << 4);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const StagePar P = par[e];
+      const unsigned msk = (unsigned)P.mask;
+      const bool jin = (msk >> (8 + jl)) & 1u;
+      const bool cover = (P.kind & WK_COVER) != 0;
+      const bool dirac = (P.kind & 7) == WK_DIRAC;
+      const float dy = (P.dyr - jlf) + P.yf;
+      const float dy2k = dy * dy * P.k2;
+#pragma unroll
+      for (int k = 0; k < PXL; ++k) {
+        const float dx = (P.dxr - ilf[k]) + P.xf;
+        const bool in = jin && ((msk >> il[k]) & 1u);
+        float u = fminf(fmaf(dx * P.k2, dx, dy2k), ucap);
+        u = (cover || in) ? u : ucap;
+        float t;
+        const float4 cf = kt_cell_smem(base32, u, t);
+        const float wt = horner3(cf, t) * P.scale;
+        w[e][k] = dirac ? (in ? P.scale : 0.f) : wt;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      w_particle<PXL>(par[e], ks, ktab_s32, ucap, wr0, il, ilf, jl, jlf, lane, w[e]);
+  }
+  const unsigned goff = (unsigned)(g8 >> 1) * 4096u + (unsigned)(g8 & 1) * 128u;
+#pragma unroll
+  for (int k = 0; k < PXL; ++k) {
+    const int m = 32 * (pg * PXL + k) + lane;
+    const float v[8] = {w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], w[6][k], w[7][k]};
+    store_row8<SPLIT>(a0, a_bytes, goff + (unsigned)(m >> 3) * 256u + (unsigned)(m & 7) * 16u,
+                      v);
+  }
+}
+
+// Spectrum-store values of one S task (8 particles at the lane's window
+// channel), loaded ahead of their store.
+__device__ __forceinline__ void s_task_load(const SPar* sp, const unsigned* spec, int wa, int n,
+                                            unsigned (&v)[8]) {
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const SPar q = sp[e];
+    const unsigned d = (unsigned)(wa + n - q.clo);  // below clo wraps past n
+    v[e] = d < q.n ? __ldg(spec + q.soff + d) : 0u;
+  }
+}
+
+// B = S of one 8-particle group at window channel n (n < nw), from values
+// as the spectrum store keeps them: hi | lo << 16 halves (pairs), or the
+// FP32 value (three pieces).
+template <int SPLIT>
+__device__ __forceinline__ void s_task_store(const unsigned (&v)[8], int g8, int n, int nw,
+                                             unsigned char* b0, unsigned b_bytes) {
+  const unsigned off = (unsigned)(g8 >> 1) * ((unsigned)nw * 32u) + (unsigned)(g8 & 1) * 128u +
+                       (unsigned)(n >> 3) * 256u + (unsigned)(n & 7) * 16u;
+  if constexpr (SPLIT == SPLIT_BF16_3) {
+    const float f[8] = {__uint_as_float(v[0]), __uint_as_float(v[1]), __uint_as_float(v[2]),
+                        __uint_as_float(v[3]), __uint_as_float(v[4]), __uint_as_float(v[5]),
+                        __uint_as_float(v[6]), __uint_as_float(v[7])};
+    store_row8<SPLIT>(b0, b_bytes, off, f);
+  } else {
+    const uint4 h = make_uint4(__byte_perm(v[0], v[1], 0x5410), __byte_perm(v[2], v[3], 0x5410),
+                               __byte_perm(v[4], v[5], 0x5410), __byte_perm(v[6], v[7], 0x5410));
+    const uint4 l = make_uint4(__byte_perm(v[0], v[1], 0x7632), __byte_perm(v[2], v[3], 0x7632),
+                               __byte_perm(v[4], v[5], 0x7632), __byte_perm(v[6], v[7], 0x7632));
+    *reinterpret_cast<uint4*>(b0 + off) = h;
+    *reinterpret_cast<uint4*>(b0 + b_bytes + off) = l;
+  }
+}
+
 // Min clo and max chi over the records of one warp's 32 particles of a
 // stage (invalid entries ignored), written by lane 0 to win[warp].
 __device__ __forceinline__ void window_partial(int (*win)[2], const PRec& r, bool valid, int warp,
@@ -823,7 +947,8 @@ __device__ __forceinline__ void window_partial(int (*win)[2], const PRec& r, boo
 template <int SPLIT, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
-  static_assert(KC == split_kc(SPLIT), "stage size of the split");
+  static_assert(KC == split_kc(SPLIT) || (KC == 32 && split_parts(SPLIT) == 2),
+                "stage size of the split");
   static_assert(KC == 32 || KC == 64, "records of a stage: one per thread of warps 0 (and 1)");
   constexpr bool BF16 = split_bf16(SPLIT);
   constexpr int NP = split_parts(SPLIT);  // 16-bit pieces per operand
@@ -836,10 +961,11 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   __shared__ __align__(16) PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
   __shared__ int s_win[2][2][2];  // [stage buffer][warp 0, 1][min clo, max chi]
-  __shared__ long long s_soff[2][KC];  // spectrum store rows
+  __shared__ __align__(16) StagePar s_par[2][KC];  // weight producers' view of a stage
+  __shared__ __align__(16) SPar s_spar[2][KC];     // spectrum producers' view
+  __shared__ int s_simple[2][KC / 8];  // 8-particle groups of table / Dirac kernels only
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
-  __shared__ float4 s_gtab[GT_NCELL + 1];  // Gaussian truncation factor
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
@@ -862,8 +988,6 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   const unsigned sbase = smem_u32(smem);
 
   if (tid < MG_MAX_KERNELS) s_ks[tid] = g.ks[tid];
-  for (int e = tid; e < GT_NCELL + 1; e += TC_THREADS)
-    s_gtab[e] = reinterpret_cast<const float4*>(gt_coef)[e];
   // the table of the launch's radial kernel (at most one per kernel tuple)
   int ktab_type = -1;
   for (int k = 0; k < g.n_kernels; ++k)
@@ -878,9 +1002,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       ktab_type = -1;
     }
   }
-  // the cubic spline's evaluator indexes cells from the start of kt_coef
-  const float4* const ktab_base =
-      s_ktab - (ktab_type >= 0 ? kt_info[ktab_type].reg[0].first : 0);
+  // the zero cell past the support of the shared-memory table
+  const float ucap = ktab_type >= 0 ? (float)kt_info[ktab_type].reg[0].ncell : 0.f;
   if (tid == 0) {
     mbar_init(smem_u32(&bars[0]), 1);
     mbar_init(smem_u32(&bars[1]), 1);
@@ -920,19 +1043,15 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   auto drain_tmem = [&](int lo, int hi) {
     for (int c = colgrp * 32; c < ncols; c += 128) {
       if (!chunk_in(c, lo, hi)) continue;
-      for (int h = 0; h < 32; h += 16) {
-        unsigned a[16], b[16];
-        tmem_ld16(tmem + lane_base + c + h, a);
-        tmem_ld16(tmem + lane_base + TC_MASTER_COL + c + h, b);
-        tmem_wait_ld();
+      unsigned a[32], b[32];
+      tmem_ld32(tmem + lane_base + c, a);
+      tmem_ld32(tmem + lane_base + TC_MASTER_COL + c, b);
+      tmem_wait_ld();
 #pragma unroll
-        for (int v = 0; v < 16; ++v) {
-          b[v] = __float_as_uint(__uint_as_float(a[v]) + __uint_as_float(b[v]));
-          a[v] = 0u;
-        }
-        tmem_st16(tmem + lane_base + TC_MASTER_COL + c + h, b);
-        tmem_st16(tmem + lane_base + c + h, a);
-      }
+      for (int v = 0; v < 32; ++v)
+        b[v] = __float_as_uint(__uint_as_float(a[v]) + __uint_as_float(b[v]));
+      tmem_st32(tmem + lane_base + TC_MASTER_COL + c, b);
+      tmem_st32_zero(tmem + lane_base + c);
     }
     tmem_wait_st();
   };
@@ -980,19 +1099,23 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
 
     // records of the first stage; the list entry of the second
     int pid_ahead = 0;
+    const int cb0 = it.c0, cb1 = it.c0 + ncols - 1;  // the segment's channel block
     if (tid < KC) {
       if (tid < it.lcount) {
         const int pid = w.list[it.lbeg + tid];
         recs[0][tid] = w.rec[pid];
         s_pid[0][tid] = pid;
-        s_soff[0][tid] = spec ? w.pair_off[pid] : 0;
+        s_spar[0][tid].soff = spec ? w.pair_off[pid] : 0;
       } else {
         recs[0][tid] = empty_rec();
         s_pid[0][tid] = 0;
-        s_soff[0][tid] = 0;
+        s_spar[0][tid].soff = 0;
       }
       if (KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + KC + tid];
       window_partial(s_win[0], recs[0][tid], tid < it.lcount, warp, lane);
+      const int kind = build_par(recs[0][tid], tid < it.lcount, i0, j0, cb0, cb1, s_ks,
+                                 ktab_type, sw, s_par[0][tid], s_spar[0][tid]);
+      group_flags(kind, tid, s_simple[0]);
     }
     __syncthreads();
 
@@ -1014,13 +1137,13 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         if (k0 + KC + tid < it.lcount) {
           const int npid = pid_ahead;
           cp_async_rec(&recs[buf ^ 1][tid], w.rec + npid);
-          if (spec) cp_async8(&s_soff[buf ^ 1][tid], w.pair_off + npid);
-          else s_soff[buf ^ 1][tid] = 0;
+          if (spec) cp_async8(&s_spar[buf ^ 1][tid].soff, w.pair_off + npid);
+          else s_spar[buf ^ 1][tid].soff = 0;
           s_pid[buf ^ 1][tid] = npid;
         } else {
           recs[buf ^ 1][tid] = empty_rec();
           s_pid[buf ^ 1][tid] = 0;
-          s_soff[buf ^ 1][tid] = 0;
+          s_spar[buf ^ 1][tid].soff = 0;
         }
         cp_async_commit();
         if (k0 + 2 * KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + tid];
@@ -1063,47 +1186,56 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         tc_fence_before();
         drain_due = false;
       };
-      // ---- A = W and B = S, particle-major: warp w owns particles
-      // w * PPW .. w * PPW + PPW - 1, taken in pairs
-      constexpr int PPW = KC / (TC_THREADS / 32);
-      // the drain runs halfway through this stage's production (after it,
-      // for one pair per warp)
-      constexpr int DRAIN_PP = PPW >= 4 ? PPW / 2 : PPW;
-#pragma unroll
-      for (int pp = 0; pp < PPW; pp += 2) {
-        if (pp == DRAIN_PP && drain_due) drain_now();  // warp-uniform
-        const int q = warp * PPW + pp;
-        const PRec r0 = recs[buf][q];
-        const PRec r1 = recs[buf][q + 1];
-        // a particle listed for this block whose line misses the block (the
-        // list bound is conservative) contributes nothing: no weights
-        const int cb0 = it.c0, cb1 = it.c0 + ncols - 1;
-        const bool v0 = q < kn && r0.chi >= cb0 && r0.clo <= cb1;
-        const bool v1 = q + 1 < kn && r1.chi >= cb0 && r1.clo <= cb1;
-        // spectrum store loads of the first 64 window channels, in flight
-        // while the weights are computed
-        unsigned pf0 = 0u, pf1 = 0u, pf2 = 0u, pf3 = 0u;
-        if (spec) {
-          const long long so0 = s_soff[buf][q], so1 = s_soff[buf][q + 1];
-          const int wa = it.c0 + w0;
-          const SpecRow q0 = spec_row(spec, so0, r0, v0), q1 = spec_row(spec, so1, r1, v1);
-          pf0 = spec_at(q0, wa + lane);
-          pf1 = spec_at(q1, wa + lane);
-          pf2 = spec_at(q0, wa + 32 + lane);
-          pf3 = spec_at(q1, wa + 32 + lane);
+      // ---- A = W: one 8-particle group x pixel group per warp
+      constexpr int PXL = KC / 32;  // pixels per lane
+      constexpr int NG8 = KC / 8;   // particle groups of a stage
+      const int wa = it.c0 + w0;    // first window channel (absolute)
+      // spectra of the warp's first S task: loads in flight during the weights
+      const int n_chunks = (nw + 31) >> 5;
+      const int n_stasks = spec ? n_chunks * NG8 : 0;
+      unsigned sv[8];
+      if (warp < n_stasks)
+        s_task_load(s_spar[buf] + 8 * (warp % NG8), spec, wa, 32 * (warp / NG8) + lane, sv);
+      produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8),
+                                 ktab_type >= 0 && s_simple[buf][warp % NG8], s_ks,
+                                 smem_u32(s_ktab), ucap, warp % NG8, warp / NG8, lane, sa, a_bytes);
+      // the drain of the previous interval: its MMAs are done by now
+      if (drain_due) drain_now();  // block-uniform
+      // ---- B = S
+      if (spec) {
+        // Gaussian lines from the spectrum store: tasks of (32-channel
+        // chunk, 8-particle group), round robin over the warps
+        for (int t = warp; t < n_stasks; t += TC_THREADS / 32) {
+          const int g8 = t % NG8, n = 32 * (t / NG8) + lane;
+          if (t != warp) s_task_load(s_spar[buf] + 8 * g8, spec, wa, n, sv);
+          if (n < nw) s_task_store<SPLIT>(sv, g8, n, nw, sb, b_bytes);
         }
-        produce_w_pair<SPLIT>(r0, r1, v0, v1, s_ks, ktab_base, smem_u32(s_ktab), ktab_type,
-                              smem_u32(s_gtab), q, i0, j0, lane, sw, sa, a_bytes);
-        produce_s_pair<SPLIT>(r0, r1, v0, v1, q, it.c0 + w0, nw, nc, dec, g.spectral_model,
-                              w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
-                              (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0),
-                              lane, ss, spec, s_soff[buf][q], s_soff[buf][q + 1], pf0, pf1, pf2,
-                              pf3, sb, b_bytes);
+      } else {
+        // lines evaluated here (Dirac lines, tabulated spectra, or no room
+        // for the store): warp w takes particles w * PPW .. + PPW - 1 in pairs
+        constexpr int PPW = KC / (TC_THREADS / 32);
+#pragma unroll
+        for (int pp = 0; pp < PPW; pp += 2) {
+          const int q = warp * PPW + pp;
+          const PRec r0 = recs[buf][q];
+          const PRec r1 = recs[buf][q + 1];
+          // a particle listed for this block whose line misses the block
+          // (the list bound is conservative) contributes nothing
+          const bool v0 = q < kn && r0.chi >= cb0 && r0.clo <= cb1;
+          const bool v1 = q + 1 < kn && r1.chi >= cb0 && r1.clo <= cb1;
+          produce_s_pair<SPLIT>(r0, r1, v0, v1, q, wa, nw, nc, dec, g.spectral_model,
+                                w.ehi + G.edge0, w.elo + G.edge0, w.inv_w + G.edge0, G.spectra,
+                                (int)(s_pid[buf][q] - G.p0), (int)(s_pid[buf][q + 1] - G.p0),
+                                lane, ss, sb, b_bytes);
+        }
       }
-      if (DRAIN_PP == PPW && drain_due) drain_now();
       if (has_next && tid < KC) {
         cp_async_wait_all();
         window_partial(s_win[buf ^ 1], recs[buf ^ 1][tid], k0 + KC + tid < it.lcount, warp, lane);
+        const int kind = build_par(recs[buf ^ 1][tid], k0 + KC + tid < it.lcount, i0, j0, cb0,
+                                   cb1, s_ks, ktab_type, sw, s_par[buf ^ 1][tid],
+                                   s_spar[buf ^ 1][tid]);
+        group_flags(kind, tid, s_simple[buf ^ 1]);
       }
       fence_proxy_async();
       __syncthreads();
@@ -1263,10 +1395,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   }
 }
 
-template <int SPLIT>
+template <int SPLIT, int KC>
 int launch_tc(const Geo& g, const Ws& w, int num_sms, cudaStream_t s, int nwmax) {
-  constexpr int KC = split_kc(SPLIT);
-  size_t smem = 2 * tc_stage_bytes(SPLIT, nwmax);
+  size_t smem = 2 * tc_stage_bytes(SPLIT, KC, nwmax);
   // at least 116 KB so that one CTA (and its 512 TMEM columns) fits per SM
   if (smem < 118784) smem = 118784;
   // the shared-memory attribute is per device: set once on each (host-side
@@ -1306,9 +1437,17 @@ void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
 int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
   const int nwmax = g.max_width;  // a stage window never exceeds the widest block
   if (nwmax > TC_MASTER_COL) return MG_ERR_UNSUPPORTED;
-  const int rc = g.form == MG_FORM_BF16X6   ? launch_tc<SPLIT_BF16_3>(g, w, num_sms, s, nwmax)
-                 : g.form == MG_FORM_BF16X3 ? launch_tc<SPLIT_BF16_2>(g, w, num_sms, s, nwmax)
-                                            : launch_tc<SPLIT_F16_2>(g, w, num_sms, s, nwmax);
+  // stage size: the form's default unless the launch shape asks for 32
+  const bool kc32 = g.kc == 32;
+  int rc;
+  if (g.form == MG_FORM_BF16X6)
+    rc = launch_tc<SPLIT_BF16_3, 32>(g, w, num_sms, s, nwmax);
+  else if (g.form == MG_FORM_BF16X3)
+    rc = kc32 ? launch_tc<SPLIT_BF16_2, 32>(g, w, num_sms, s, nwmax)
+              : launch_tc<SPLIT_BF16_2, 64>(g, w, num_sms, s, nwmax);
+  else
+    rc = kc32 ? launch_tc<SPLIT_F16_2, 32>(g, w, num_sms, s, nwmax)
+              : launch_tc<SPLIT_F16_2, 64>(g, w, num_sms, s, nwmax);
   if (rc) return rc;
   launch_reduce_partials(g, w, num_sms, s);
   return MG_OK;

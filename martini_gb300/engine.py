@@ -117,6 +117,23 @@ class InsertionEngine:
         self.last_plan = info
         return info
 
+    def tune(self, prob: N.Problem, reps: int = 3, stream=None) -> dict:
+        """Autotune the launch shape of ``prob`` (after :meth:`plan`): every
+        candidate is binned and its contraction timed ``reps`` times; the
+        fastest is cached for the problem's class, so later runs and
+        captures of this (or a like) problem use it.  Synchronises and
+        overwrites the cube.  Returns the shape and its median time (ms)."""
+        s = stream or torch.cuda.current_stream(self.device)
+        ws = self._ws
+        best = N.Tuning()
+        ms = C.c_float()
+        N.check(self.lib.mg_tune(C.byref(prob), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                 self._caps[0], self._caps[1], int(reps),
+                                 C.c_void_p(s.cuda_stream), C.byref(best), C.byref(ms)))
+        out = best.as_dict()
+        out["contract_ms"] = float(ms.value)
+        return out
+
     def run(self, prob: N.Problem, stream=None) -> None:
         """Full insertion with the capacities of the last plan (asynchronous)."""
         s = stream or torch.cuda.current_stream(self.device)
@@ -224,6 +241,19 @@ class BatchInsertion:
         self._workspace(int(info.workspace_bytes))
         self.last_plan = info
         return info
+
+    def tune(self, reps: int = 3, stream=None) -> dict:
+        """Autotune the batch's launch shape (after :meth:`plan`; see
+        :meth:`InsertionEngine.tune`): synchronises and overwrites the cubes."""
+        ws = self._ws
+        best = N.Tuning()
+        ms = C.c_float()
+        N.check(self.lib.mg_tune_batched(self.arr, self.n, C.c_void_p(ws.data_ptr()), ws.numel(),
+                                         self._caps[0], self._caps[1], int(reps),
+                                         self._stream(stream), C.byref(best), C.byref(ms)))
+        out = best.as_dict()
+        out["contract_ms"] = float(ms.value)
+        return out
 
     def run(self, stream=None) -> None:
         ws = self._ws

@@ -144,10 +144,19 @@ class _BaseMartini:
         else:
             dc._array += add / px2
         dc._array_unit = "Jy/arcsec2"
+        # this insertion's FP64 flux sums over the unpadded cube (total, then
+        # per channel), from the GPU
         self._last_flux = flux
-        inserted_flux = float(flux[0])
+        # the summary sums the whole converted array, prior contents
+        # included, over the unpadded pixels when both pads are non-zero
+        # (martini/martini.py:367-392)
+        pad_mask = (np.s_[dc.padx:-dc.padx, dc.pady:-dc.pady, ...]
+                    if dc.padx > 0 and dc.pady > 0 else np.s_[...])
+        in_jy = dc._array[pad_mask] * px2
+        inserted_flux = float(np.sum(in_jy))
+        per_channel = in_jy.sum(axis=(0, 1)).reshape(-1)
         inserted_mass = MHI_TO_JY * self.source.distance**2 * float(
-            np.sum(flux[1:] * np.abs(np.diff(dc.velocity_channel_edges))))
+            np.sum(per_channel * np.abs(np.diff(dc.velocity_channel_edges))))
         self.inserted_flux_density = inserted_flux
         self.inserted_mass = inserted_mass
         if (quiet is None and not self.quiet) or (quiet is not None and not quiet):

@@ -131,8 +131,14 @@ def test_insert_accumulates_into_existing_array():
                 spectral_model=GaussianSpectrum(), quiet=True)
     m.insert_source_in_cube()
     once = dc._array.copy()
+    f1, m1 = m.inserted_flux_density, m.inserted_mass
     m.insert_source_in_cube()
     np.testing.assert_allclose(dc._array, 2 * once, rtol=1e-12)
+    # the summary sums the whole array, the first insertion included
+    # (martini/martini.py:367-392)
+    assert m.inserted_flux_density == pytest.approx(2 * f1, rel=1e-12)
+    assert m.inserted_mass == pytest.approx(2 * m1, rel=1e-12)
+    assert f1 == pytest.approx(float(m._last_flux[0]), rel=1e-6)
     m.reset()
     assert dc._array.sum() == 0
     m.insert_source_in_cube()

@@ -186,3 +186,68 @@ def test_population_configs_are_seeded_and_in_range():
     assert W.population_configs(5) == cf[:5]
     g = W.build_population(2)
     assert len(g) == 2 and all(x["n"] > 0 for x in g)
+
+
+def _ref_rotmat(ra_deg, dec_deg):
+    """The rotation the reference's tests expect: R_y(dec) . R_z(-ra), on
+    row vectors (tests/test_sources.py:233-262)."""
+    ra, dec = np.deg2rad(ra_deg), np.deg2rad(dec_deg)
+    R_y = np.array([[np.cos(dec), 0, np.sin(dec)], [0, 1, 0], [-np.sin(dec), 0, np.cos(dec)]])
+    R_z = np.array([[np.cos(-ra), -np.sin(-ra), 0], [np.sin(-ra), np.cos(-ra), 0], [0, 0, 1]])
+    return R_y.dot(R_z)
+
+
+def _sky(pos, vel):
+    d = np.sqrt((pos ** 2).sum(axis=1))
+    return (np.rad2deg(np.arctan2(pos[:, 1], pos[:, 0])) % 360.0,
+            np.rad2deg(np.arcsin(pos[:, 2] / d)), d, (pos * vel).sum(axis=1) / d)
+
+
+@pytest.mark.parametrize("ra", [0.0, 30.0, -30.0])
+@pytest.mark.parametrize("dec", [0.0, 30.0, -30.0])
+@pytest.mark.parametrize("distance", [0.0, 3.0])
+@pytest.mark.parametrize("vpeculiar", [0.0, 100.0])
+def test_sky_placement_known_answer(ra, dec, distance, vpeculiar):
+    """tests/test_sources.py:268-316 (and :231-266 at distance 0, h = 0):
+    positions rotate by R_y(dec) R_z(-ra), translate by the distance along
+    the rotated x axis, and velocities gain the peculiar velocity along it
+    and the Hubble flow h 100 km/s/Mpc times each particle's distance."""
+    xyz = np.arange(1, 4, dtype=float).reshape(1, 3) * np.array([[1.0], [2.0]])
+    vxyz = np.arange(1, 4, dtype=float).reshape(1, 3) * np.array([[1.0], [-1.0]])
+    src = SPHSource(xyz_g=xyz, vxyz_g=vxyz, mHI_g=np.ones(2), ra=ra, dec=dec,
+                    distance=distance, vpeculiar=vpeculiar)
+    src._init_skycoords()
+    rot = _ref_rotmat(ra, dec)
+    direction = rot.T.dot(np.array([[1.0], [0.0], [0.0]]))
+    pos = xyz.dot(rot) + direction.T * distance * 1e3             # kpc
+    dist = np.sqrt((pos ** 2).sum(axis=1))
+    vel = (vxyz.dot(rot) + pos / dist[:, None] * (0.7 * 100 * dist * 1e-3)[:, None]
+           + (direction * vpeculiar).T)
+    ra_e, dec_e, d_e, v_e = _sky(pos, vel)
+    np.testing.assert_allclose(src.skycoords.ra, ra_e, atol=1e-9)
+    np.testing.assert_allclose(src.skycoords.dec, dec_e, atol=1e-9)
+    np.testing.assert_allclose(src.skycoords.distance, d_e * 1e-3, rtol=1e-12)
+    np.testing.assert_allclose(src.skycoords.radial_velocity, v_e, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("ra", [0.0, 30.0, -30.0])
+@pytest.mark.parametrize("dec", [0.0, 30.0, -30.0])
+def test_sky_location_known_answer(ra, dec):
+    """tests/test_sources.py:381-395: a particle at the origin lands at the
+    source's (ra, dec); on a cube centred there (datacube.py:438-486) its
+    pixel is the reference pixel, and a particle 1 kpc along +y (+RA on the
+    sky, RA pixel axis decreasing) one arcsec-at-D away lands one pixel off."""
+    D = 1e-3 / np.deg2rad(1 / 3600.0)  # 1 kpc subtends 1 arcsec
+    src = SPHSource(xyz_g=np.array([[0.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]]),
+                    vxyz_g=np.zeros((3, 3)), mHI_g=np.ones(3), ra=ra, dec=dec, distance=D, h=0.0,
+                    coordinate_axis=1)
+    src._init_skycoords()
+    assert src.skycoords.ra[0] == pytest.approx(ra % 360.0, abs=1e-9)
+    assert src.skycoords.dec[0] == pytest.approx(dec, abs=1e-9)
+    dc = DataCube(n_px_x=8, n_px_y=8, n_channels=4, px_size=1.0, channel_width=1.0, ra=ra,
+                  dec=dec)
+    src._init_pixcoords(dc)
+    np.testing.assert_allclose(src.pixcoords[:2, 0], [3.5, 3.5], atol=1e-9)
+    # offsets of 1 arcsec along the source's sky axes, to TAN's second order
+    np.testing.assert_allclose(src.pixcoords[:2, 1], [2.5, 3.5], atol=1e-4)
+    np.testing.assert_allclose(src.pixcoords[:2, 2], [3.5, 4.5], atol=1e-4)

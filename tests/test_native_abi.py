@@ -12,7 +12,7 @@ LIB = os.path.join(ROOT, "martini_gb300", "libmartini_gb300.so")
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:const char\*|int|size_t)\s+(mg_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:const char\*|int|size_t|void)\s+(mg_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_entry_points():
