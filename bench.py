@@ -577,6 +577,8 @@ def e2e_time(a, w, ins, cube, flux, form, edges, dev, stream):
         st["host_flux"] = torch.empty(nc + 1, dtype=torch.float64).pin_memory()
     h2d = sum(t.numel() * t.element_size() for g in ins for t in g["host"].values())
     d2h = sets[0]["host_cube"].numel() * 4 + sets[0]["host_flux"].numel() * 8
+    nslab = 8 if nx >= 8 else 1
+    slabs = [(nx * i // nslab, nx * (i + 1) // nslab) for i in range(nslab)]
     up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     comp_ev, down_ev = {}, {}
 
@@ -598,7 +600,10 @@ def e2e_time(a, w, ins, cube, flux, form, edges, dev, stream):
         comp_ev[k] = stream.record_event()
         down.wait_event(comp_ev[k])
         with torch.cuda.stream(down):
-            st["host_cube"].copy_(st["cube"], non_blocking=True)
+            # in slabs of rows: one copy of the whole 2 GB cube runs far below
+            # the link's device-to-host rate, eight of them near it
+            for a, b in slabs:
+                st["host_cube"][a:b].copy_(st["cube"][a:b], non_blocking=True)
             st["host_flux"].copy_(st["flux"], non_blocking=True)
         down_ev[k] = down.record_event()
 
@@ -634,7 +639,10 @@ def run_population(a, rank, world, local, dev):
     from martini_gb300.engine import BatchInsertion, DeviceParticles, InsertionEngine
 
     form = FORMS[a.form]
-    gals_all = workloads.build_population(a.n_gal, workers=0)
+    # large populations are set up in a spawn-started process pool (numpy
+    # host set-up of up to 2000 galaxies; no GPU work in the workers)
+    nw = min(8, os.cpu_count() or 1) if a.n_gal > 200 else 0
+    gals_all = workloads.build_population(a.n_gal, workers=nw)
     gals = gals_all
     imbalance = None
     if world > 1:
