@@ -641,7 +641,7 @@ struct SPar {
 };
 
 // StagePar / SPar of one particle of a stage (valid: listed for this stage;
-// the record of an unused slot is empty).  Returns the WK_* kind.
+// the record of an unused slot is empty).  Returns the WK_* kind and flags.
 __device__ __forceinline__ int build_par(const PRec& r, bool valid, int i0, int j0, int cb0,
                                          int cb1, const KSpec* ks, int ktab_type, float sw,
                                          StagePar& P, SPar& S) {
@@ -694,17 +694,27 @@ __device__ __forceinline__ int build_par(const PRec& r, bool valid, int i0, int 
   P.mask = (int)(rows | cols << 8);
   S.clo = r.clo;
   S.n = (valid && r.chi >= r.clo) ? (unsigned)(r.chi - r.clo + 1) : 0u;
-  return kind & 7;
+  return kind;
 }
 
-// The group flags of a stage's particles, one thread per particle (whole
-// warps; lanes 8 g .. 8 g + 7 hold group g of the warp): 1 when all eight
-// are WK_NONE, WK_TAB or WK_DIRAC.
+// Group paths of the weight producers.
+constexpr int GP_GENERAL = 0;  // each particle takes its kind's path
+constexpr int GP_MIXED = 1;    // table / Dirac / empty: one branch-free block with box tests
+constexpr int GP_COVERED = 2;  // table kernels whose boxes hold their supports, or empty
+
+// The group paths of a stage's particles, one thread per particle (whole
+// warps; lanes 8 g .. 8 g + 7 hold group g of the warp).
 __device__ __forceinline__ void group_flags(int kind, int tid, int* flags) {
-  const bool simple = kind == WK_NONE || kind == WK_TAB || kind == WK_DIRAC;
-  const unsigned bal = __ballot_sync(0xffffffffu, simple);
+  const int k = kind & 7;
+  const bool covered = k == WK_NONE || (k == WK_TAB && (kind & WK_COVER));
+  const bool mixed = k == WK_NONE || k == WK_TAB || k == WK_DIRAC;
+  const unsigned bc = __ballot_sync(0xffffffffu, covered);
+  const unsigned bm = __ballot_sync(0xffffffffu, mixed);
   const int lane = tid & 31;
-  if ((lane & 7) == 0) flags[tid >> 3] = ((bal >> lane) & 0xFFu) == 0xFFu;
+  if ((lane & 7) == 0)
+    flags[tid >> 3] = ((bc >> lane) & 0xFFu) == 0xFFu   ? GP_COVERED
+                      : ((bm >> lane) & 0xFFu) == 0xFFu ? GP_MIXED
+                                                         : GP_GENERAL;
 }
 
 __device__ __forceinline__ float horner3(const float4& cf, float t) {
@@ -835,13 +845,15 @@ __device__ __forceinline__ void store_row8(unsigned char* base, unsigned piece_b
   }
 }
 
-// A = W of one 8-particle group over the warp's pixel group.  `simple`: every
-// particle of the group is WK_NONE, WK_TAB or WK_DIRAC, so the 8 x PXL
-// weights are one branch-free block of independent chains (NONE: empty
-// mask and zero scale, which the table's zero cell turns into 0; DIRAC: the
-// box test picks sw); otherwise each particle takes its kind's path.
+// A = W of one 8-particle group over the warp's pixel group.  `path`
+// GP_COVERED: every particle is empty or a table kernel whose box holds its
+// support, so the 8 x PXL weights are one branch-free block of independent
+// chains with no box test (an empty slot has zero k2 and scale: u = 0 and a
+// zero weight).  GP_MIXED adds Dirac particles and box tests (an empty
+// slot's mask is empty, so u lands on the table's zero cell; DIRAC: the box
+// test picks sw).  GP_GENERAL: each particle takes its kind's path.
 template <int SPLIT, int PXL>
-__device__ __forceinline__ void produce_w_task(const StagePar* par, bool simple, const KSpec* ks,
+__device__ __forceinline__ void produce_w_task(const StagePar* par, int path, const KSpec* ks,
                                                unsigned ktab_s32, float ucap, int g8, int pg,
                                                int lane, unsigned char* a0, unsigned a_bytes) {
   const int jl = lane & 15;
@@ -855,7 +867,23 @@ __device__ __forceinline__ void produce_w_task(const StagePar* par, bool simple,
     ilf[k] = (float)il[k];
   }
   float w[8][PXL];
-  if (simple) {
+  if (path == GP_COVERED) {
+    const unsigned base32 = ktab_s32 - (0x4B000000u << 4);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const StagePar P = par[e];
+      const float dy = (P.dyr - jlf) + P.yf;
+      const float dy2k = dy * dy * P.k2;
+#pragma unroll
+      for (int k = 0; k < PXL; ++k) {
+        const float dx = (P.dxr - ilf[k]) + P.xf;
+        const float u = fminf(fmaf(dx * P.k2, dx, dy2k), ucap);
+        float t;
+        const float4 cf = kt_cell_smem(base32, u, t);
+        w[e][k] = horner3(cf, t) * P.scale;
+      }
+    }
+  } else if (path == GP_MIXED) {
     const unsigned base32 = ktab_s32 - (0x4B000000u << 4);
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
@@ -963,7 +991,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   __shared__ int s_win[2][2][2];  // [stage buffer][warp 0, 1][min clo, max chi]
   __shared__ __align__(16) StagePar s_par[2][KC];  // weight producers' view of a stage
   __shared__ __align__(16) SPar s_spar[2][KC];     // spectrum producers' view
-  __shared__ int s_simple[2][KC / 8];  // 8-particle groups of table / Dirac kernels only
+  __shared__ int s_simple[2][KC / 8];  // GP_* path of each 8-particle group
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
   __shared__ __align__(8) unsigned long long bars[2];
@@ -1190,14 +1218,18 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       constexpr int PXL = KC / 32;  // pixels per lane
       constexpr int NG8 = KC / 8;   // particle groups of a stage
       const int wa = it.c0 + w0;    // first window channel (absolute)
-      // spectra of the warp's first S task: loads in flight during the weights
+      // spectrum tasks go round robin from the first warp after the record
+      // warps (which also turn the next stage's records into parameters);
+      // the loads of a warp's first task are in flight during its weights
       const int n_chunks = (nw + 31) >> 5;
       const int n_stasks = spec ? n_chunks * NG8 : 0;
+      constexpr int NWARP = TC_THREADS / 32;
+      const int t0 = (warp + NWARP - RWARPS) % NWARP;
       unsigned sv[8];
-      if (warp < n_stasks)
-        s_task_load(s_spar[buf] + 8 * (warp % NG8), spec, wa, 32 * (warp / NG8) + lane, sv);
+      if (t0 < n_stasks)
+        s_task_load(s_spar[buf] + 8 * (t0 % NG8), spec, wa, 32 * (t0 / NG8) + lane, sv);
       produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8),
-                                 ktab_type >= 0 && s_simple[buf][warp % NG8], s_ks,
+                                 ktab_type >= 0 ? s_simple[buf][warp % NG8] : GP_GENERAL, s_ks,
                                  smem_u32(s_ktab), ucap, warp % NG8, warp / NG8, lane, sa, a_bytes);
       // the drain of the previous interval: its MMAs are done by now
       if (drain_due) drain_now();  // block-uniform
@@ -1205,9 +1237,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (spec) {
         // Gaussian lines from the spectrum store: tasks of (32-channel
         // chunk, 8-particle group), round robin over the warps
-        for (int t = warp; t < n_stasks; t += TC_THREADS / 32) {
+        for (int t = t0; t < n_stasks; t += NWARP) {
           const int g8 = t % NG8, n = 32 * (t / NG8) + lane;
-          if (t != warp) s_task_load(s_spar[buf] + 8 * g8, spec, wa, n, sv);
+          if (t != t0) s_task_load(s_spar[buf] + 8 * g8, spec, wa, n, sv);
           if (n < nw) s_task_store<SPLIT>(sv, g8, n, nw, sb, b_bytes);
         }
       } else {
