@@ -577,8 +577,6 @@ def e2e_time(a, w, ins, cube, flux, form, edges, dev, stream):
         st["host_flux"] = torch.empty(nc + 1, dtype=torch.float64).pin_memory()
     h2d = sum(t.numel() * t.element_size() for g in ins for t in g["host"].values())
     d2h = sets[0]["host_cube"].numel() * 4 + sets[0]["host_flux"].numel() * 8
-    nslab = 8 if nx >= 8 else 1
-    slabs = [(nx * i // nslab, nx * (i + 1) // nslab) for i in range(nslab)]
     up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     comp_ev, down_ev = {}, {}
 
@@ -600,10 +598,7 @@ def e2e_time(a, w, ins, cube, flux, form, edges, dev, stream):
         comp_ev[k] = stream.record_event()
         down.wait_event(comp_ev[k])
         with torch.cuda.stream(down):
-            # in slabs of rows: one copy of the whole 2 GB cube runs far below
-            # the link's device-to-host rate, eight of them near it
-            for a, b in slabs:
-                st["host_cube"][a:b].copy_(st["cube"][a:b], non_blocking=True)
+            st["host_cube"].copy_(st["cube"], non_blocking=True)
             st["host_flux"].copy_(st["flux"], non_blocking=True)
         down_ev[k] = down.record_event()
 
