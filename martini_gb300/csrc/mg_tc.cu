@@ -702,19 +702,15 @@ constexpr int GP_GENERAL = 0;  // each particle takes its kind's path
 constexpr int GP_MIXED = 1;    // table / Dirac / empty: one branch-free block with box tests
 constexpr int GP_COVERED = 2;  // table kernels whose boxes hold their supports, or empty
 
-// The group paths of a stage's particles, one thread per particle (whole
-// warps; lanes 8 g .. 8 g + 7 hold group g of the warp).
-__device__ __forceinline__ void group_flags(int kind, int tid, int* flags) {
+// The path of an 8-particle group from its particles' kinds (called by a
+// whole warp; lane l looks at particle l % 8).
+__device__ __forceinline__ int group_path(const int* kinds, int lane) {
+  const int kind = kinds[lane & 7];
   const int k = kind & 7;
   const bool covered = k == WK_NONE || (k == WK_TAB && (kind & WK_COVER));
   const bool mixed = k == WK_NONE || k == WK_TAB || k == WK_DIRAC;
-  const unsigned bc = __ballot_sync(0xffffffffu, covered);
-  const unsigned bm = __ballot_sync(0xffffffffu, mixed);
-  const int lane = tid & 31;
-  if ((lane & 7) == 0)
-    flags[tid >> 3] = ((bc >> lane) & 0xFFu) == 0xFFu   ? GP_COVERED
-                      : ((bm >> lane) & 0xFFu) == 0xFFu ? GP_MIXED
-                                                         : GP_GENERAL;
+  if (__all_sync(0xffffffffu, covered)) return GP_COVERED;
+  return __all_sync(0xffffffffu, mixed) ? GP_MIXED : GP_GENERAL;
 }
 
 __device__ __forceinline__ float horner3(const float4& cf, float t) {
@@ -956,20 +952,22 @@ __device__ __forceinline__ void s_task_store(const unsigned (&v)[8], int g8, int
   }
 }
 
-// Min clo and max chi over the records of one warp's 32 particles of a
-// stage (invalid entries ignored), written by lane 0 to win[warp].
-__device__ __forceinline__ void window_partial(int (*win)[2], const PRec& r, bool valid, int warp,
-                                               int lane) {
-  int lo = valid ? r.clo : 0x7fffffff, hi = valid ? r.chi : -1;
+// Min clo and max chi over a stage's KC particles (listed slots; others
+// hold an empty range), reduced by a whole warp.
+template <int KC>
+__device__ __forceinline__ int2 stage_window(const int2* lohi, int lane) {
+  int2 v = lohi[lane];
+  if (KC > 32) {
+    const int2 u = lohi[lane + 32];
+    v.x = min(v.x, u.x);
+    v.y = max(v.y, u.y);
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    v.x = min(v.x, __shfl_xor_sync(0xffffffffu, v.x, o));
+    v.y = max(v.y, __shfl_xor_sync(0xffffffffu, v.y, o));
   }
-  if (lane == 0) {
-    win[warp][0] = lo;
-    win[warp][1] = hi;
-  }
+  return v;
 }
 
 template <int SPLIT, int KC>
@@ -977,10 +975,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
   static_assert(KC == split_kc(SPLIT) || (KC == 32 && split_parts(SPLIT) == 2),
                 "stage size of the split");
-  static_assert(KC == 32 || KC == 64, "records of a stage: one per thread of warps 0 (and 1)");
+  static_assert(KC == 32 || KC == 64, "records of a stage: KC / 16 lanes of every warp");
   constexpr bool BF16 = split_bf16(SPLIT);
   constexpr int NP = split_parts(SPLIT);  // 16-bit pieces per operand
-  constexpr int RWARPS = KC / 32;         // warps that copy a stage's records
+  // A stage's records are handled by the first RPW lanes of every warp (record
+  // slot rq = warp * RPW + lane), so that copying them and turning them into
+  // parameters adds the same few instructions to every warp.
+  constexpr int RPW = KC / (TC_THREADS / 32);
   // stages between drains: TC_DRAIN for pairs (24 MMAs), every stage for
   // three pieces (the same 24 MMAs, over half the particles)
   constexpr int DRAIN_STAGES = NP == 3 ? 1 : TC_DRAIN;
@@ -988,10 +989,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(16) PRec recs[2][KC];
   __shared__ int s_pid[2][KC];
-  __shared__ int s_win[2][2][2];  // [stage buffer][warp 0, 1][min clo, max chi]
+  __shared__ int2 s_lohi[2][KC];   // support [clo, chi] of each listed particle (window)
   __shared__ __align__(16) StagePar s_par[2][KC];  // weight producers' view of a stage
   __shared__ __align__(16) SPar s_spar[2][KC];     // spectrum producers' view
-  __shared__ int s_simple[2][KC / 8];  // GP_* path of each 8-particle group
+  __shared__ int s_kind[2][KC];    // WK_* kind and flags of each particle
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
   __shared__ __align__(8) unsigned long long bars[2];
@@ -1001,6 +1002,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
+  const bool rec_lane = lane < RPW;  // this thread handles record slot rq
+  const int rq = warp * RPW + lane;
   if (w.hdr->status) return;
   const long long n_items = w.hdr->n_items;
   const int kch = w.hdr->kch;
@@ -1128,22 +1131,23 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     // records of the first stage; the list entry of the second
     int pid_ahead = 0;
     const int cb0 = it.c0, cb1 = it.c0 + ncols - 1;  // the segment's channel block
-    if (tid < KC) {
-      if (tid < it.lcount) {
-        const int pid = w.list[it.lbeg + tid];
-        recs[0][tid] = w.rec[pid];
-        s_pid[0][tid] = pid;
-        s_spar[0][tid].soff = spec ? w.pair_off[pid] : 0;
+    if (rec_lane) {
+      const bool listed = rq < it.lcount;
+      if (listed) {
+        const int pid = w.list[it.lbeg + rq];
+        recs[0][rq] = w.rec[pid];
+        s_pid[0][rq] = pid;
+        s_spar[0][rq].soff = spec ? w.pair_off[pid] : 0;
       } else {
-        recs[0][tid] = empty_rec();
-        s_pid[0][tid] = 0;
-        s_spar[0][tid].soff = 0;
+        recs[0][rq] = empty_rec();
+        s_pid[0][rq] = 0;
+        s_spar[0][rq].soff = 0;
       }
-      if (KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + KC + tid];
-      window_partial(s_win[0], recs[0][tid], tid < it.lcount, warp, lane);
-      const int kind = build_par(recs[0][tid], tid < it.lcount, i0, j0, cb0, cb1, s_ks,
-                                 ktab_type, sw, s_par[0][tid], s_spar[0][tid]);
-      group_flags(kind, tid, s_simple[0]);
+      if (KC + rq < it.lcount) pid_ahead = w.list[it.lbeg + KC + rq];
+      const PRec& r = recs[0][rq];
+      s_lohi[0][rq] = listed ? make_int2(r.clo, r.chi) : make_int2(0x7fffffff, -1);
+      s_kind[0][rq] = build_par(r, listed, i0, j0, cb0, cb1, s_ks, ktab_type, sw, s_par[0][rq],
+                                s_spar[0][rq]);
     }
     __syncthreads();
 
@@ -1161,30 +1165,27 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       // this one is produced (its list entry was read a stage earlier); the
       // list entry of the stage after is read now
       const bool has_next = ch + 1 < nchunk;
-      if (has_next && tid < KC) {
-        if (k0 + KC + tid < it.lcount) {
+      if (has_next && rec_lane) {
+        if (k0 + KC + rq < it.lcount) {
           const int npid = pid_ahead;
-          cp_async_rec(&recs[buf ^ 1][tid], w.rec + npid);
-          if (spec) cp_async8(&s_spar[buf ^ 1][tid].soff, w.pair_off + npid);
-          else s_spar[buf ^ 1][tid].soff = 0;
-          s_pid[buf ^ 1][tid] = npid;
+          cp_async_rec(&recs[buf ^ 1][rq], w.rec + npid);
+          if (spec) cp_async8(&s_spar[buf ^ 1][rq].soff, w.pair_off + npid);
+          else s_spar[buf ^ 1][rq].soff = 0;
+          s_pid[buf ^ 1][rq] = npid;
         } else {
-          recs[buf ^ 1][tid] = empty_rec();
-          s_pid[buf ^ 1][tid] = 0;
-          s_spar[buf ^ 1][tid].soff = 0;
+          recs[buf ^ 1][rq] = empty_rec();
+          s_pid[buf ^ 1][rq] = 0;
+          s_spar[buf ^ 1][rq].soff = 0;
         }
         cp_async_commit();
-        if (k0 + 2 * KC + tid < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + tid];
+        if (k0 + 2 * KC + rq < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + rq];
       }
       // stage channel window [w0, w0 + nw): min clo, max chi
       int w0, nw;
       {
-        // the extremes reduced by the record warps when the records arrived
-        int lo = s_win[buf][0][0], hi = s_win[buf][0][1];
-        if (RWARPS > 1) {
-          lo = min(lo, s_win[buf][1][0]);
-          hi = max(hi, s_win[buf][1][1]);
-        }
+        // the extremes of the stage's listed particles' supports
+        const int2 lh = stage_window<KC>(s_lohi[buf], lane);
+        int lo = lh.x, hi = lh.y;
         // relative to the segment's block [c0, c0 + ncols)
         lo = max(lo, it.c0) - it.c0;
         hi = min(hi, it.c0 + ncols - 1) - it.c0;
@@ -1218,18 +1219,19 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       constexpr int PXL = KC / 32;  // pixels per lane
       constexpr int NG8 = KC / 8;   // particle groups of a stage
       const int wa = it.c0 + w0;    // first window channel (absolute)
-      // spectrum tasks go round robin from the first warp after the record
-      // warps (which also turn the next stage's records into parameters);
-      // the loads of a warp's first task are in flight during its weights
+      // spectrum tasks go round robin over the warps; the loads of a warp's
+      // first task are in flight during its weights
       const int n_chunks = (nw + 31) >> 5;
       const int n_stasks = spec ? n_chunks * NG8 : 0;
       constexpr int NWARP = TC_THREADS / 32;
-      const int t0 = (warp + NWARP - RWARPS) % NWARP;
+      const int t0 = warp;
       unsigned sv[8];
       if (t0 < n_stasks)
         s_task_load(s_spar[buf] + 8 * (t0 % NG8), spec, wa, 32 * (t0 / NG8) + lane, sv);
       produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8),
-                                 ktab_type >= 0 ? s_simple[buf][warp % NG8] : GP_GENERAL, s_ks,
+                                 ktab_type >= 0 ? group_path(s_kind[buf] + 8 * (warp % NG8), lane)
+                                                : GP_GENERAL,
+                                 s_ks,
                                  smem_u32(s_ktab), ucap, warp % NG8, warp / NG8, lane, sa, a_bytes);
       // the drain of the previous interval: its MMAs are done by now
       if (drain_due) drain_now();  // block-uniform
@@ -1261,13 +1263,13 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
                                 lane, ss, sb, b_bytes);
         }
       }
-      if (has_next && tid < KC) {
+      if (has_next && rec_lane) {
         cp_async_wait_all();
-        window_partial(s_win[buf ^ 1], recs[buf ^ 1][tid], k0 + KC + tid < it.lcount, warp, lane);
-        const int kind = build_par(recs[buf ^ 1][tid], k0 + KC + tid < it.lcount, i0, j0, cb0,
-                                   cb1, s_ks, ktab_type, sw, s_par[buf ^ 1][tid],
-                                   s_spar[buf ^ 1][tid]);
-        group_flags(kind, tid, s_simple[buf ^ 1]);
+        const bool listed = k0 + KC + rq < it.lcount;
+        const PRec& r = recs[buf ^ 1][rq];
+        s_lohi[buf ^ 1][rq] = listed ? make_int2(r.clo, r.chi) : make_int2(0x7fffffff, -1);
+        s_kind[buf ^ 1][rq] = build_par(r, listed, i0, j0, cb0, cb1, s_ks, ktab_type, sw,
+                                        s_par[buf ^ 1][rq], s_spar[buf ^ 1][rq]);
       }
       fence_proxy_async();
       __syncthreads();
