@@ -61,8 +61,8 @@ def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal
     tile scan (3), plan, emit, radix passes x (histogram, scan (3), scatter),
     segments, item and partial scans (2 x 3), work-queue keys and their two
     radix passes (2 x 5), partial check, [spectrum store: row lengths, scan
-    (3), rows], [cube clear for batches], contraction, split-K reduction,
-    flux (3)."""
+    (3), rows], [cube clear for batches], [tensor-core parameters],
+    contraction, split-K reduction, flux (3)."""
     if ntiles is None:
         ntiles = ((nx + 7) // 8) * ((ny + 15) // 16)  # 8 x 16-pixel tiles
     bits = max(ntiles - 1, 0).bit_length() + max(nc - 1, 0).bit_length()
@@ -70,6 +70,8 @@ def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal
     n = (ngal + 15) // 16 + 1 + 1 + 1 + 3 + 1 + 3 + 1 + 1 + 5 * passes + 1 + 6 + 1 + 10 + 1
     if form != "fp32" and gaussian:
         n += 1 + 3 + 1
+    if form != "fp32":
+        n += 1
     if ngal > 1:
         n += 1
     return n + 1 + 1 + 3

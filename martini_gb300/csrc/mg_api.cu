@@ -62,7 +62,7 @@ int channel_bits(int nc) {
 }
 
 struct Layout {
-  size_t hdr, gal, gst, gp0, gt0, gs0, ge0, gr0, rec, npairs, pair_off, tile_count, tile_diff,
+  size_t hdr, gal, gst, gp0, gt0, gs0, ge0, gr0, rec, tpar, npairs, pair_off, tile_count, tile_diff,
       tile_off, ehi, elo, inv_w, keys, list, keys_tmp, list_tmp, rs_hist,
       rs_off, scan_sums, seg_lo, seg_hi, seg_items, seg_part, item_off, part_off, partial,
       flux_part, item_order, item_key, item_key_tmp, item_order_tmp, total;
@@ -94,6 +94,8 @@ Layout layout(const Geo& g, long long cap_pairs, long long cap_partial) {
   L.ge0 = take(sizeof(int) * ng1);
   L.gr0 = take(sizeof(int) * ng1);
   L.rec = take(sizeof(PRec) * nn);
+  const bool tc = g.form == MG_FORM_BF16X3 || g.form == MG_FORM_F16X3 || g.form == MG_FORM_BF16X6;
+  L.tpar = tc ? take(sizeof(TcPar) * nn) : 0;
   L.npairs = take(sizeof(int) * nn);
   L.pair_off = take(sizeof(long long) * nn);
   L.tile_count = take(sizeof(int) * (size_t)g.ntiles);
@@ -140,6 +142,7 @@ Ws make_ws(void* base, const Layout& L) {
   w.ge0 = reinterpret_cast<int*>(b + L.ge0);
   w.gr0 = reinterpret_cast<int*>(b + L.gr0);
   w.rec = reinterpret_cast<PRec*>(b + L.rec);
+  w.tpar = L.tpar ? reinterpret_cast<TcPar*>(b + L.tpar) : nullptr;
   w.npairs = reinterpret_cast<int*>(b + L.npairs);
   w.pair_off = reinterpret_cast<long long*>(b + L.pair_off);
   w.tile_count = reinterpret_cast<int*>(b + L.tile_count);

@@ -60,6 +60,27 @@ constexpr int PREC_ROWS_COVER = 1;
 // The same for the footprint's columns [jlo, jhi] (axis 1).
 constexpr int PREC_COLS_COVER = 2;
 
+// Per-particle parameters of the tensor-core producers (64 bytes), written
+// once per insertion by k_tc_params: the particle's position, the weight
+// constants of its kernel with the cube's operand scale applied, its kind,
+// footprint box, channel support and spectrum-store row.  The contraction
+// copies one per tile visit (four 16-byte cp.async) and derives only the
+// tile-relative fields.
+struct TcPar {
+  int xi, yi;              // floor(x), floor(y)
+  float xf, yf;            // x - xi, y - yi
+  float k2;                // table kernels: inv_h2 * cells per unit s; cubic spline: 4 inv_h2;
+                           // Gaussian: 1 / (h sigma)
+  float scale;             // weight scale with the cube's operand scale
+  int kind;                // producer kind and flags, kernel slot << 8, type << 12 (0: none)
+  int clo;                 // channel support [clo, chi]
+  int ilo, ihi, jlo, jhi;  // footprint box (clipped to the cube)
+  int chi;
+  int pad_;
+  long long soff;          // spectrum-store row of the particle
+};
+static_assert(sizeof(TcPar) == 64, "four 16-byte pieces");
+
 struct KSpec {
   int type;
   float truncate;
@@ -191,6 +212,7 @@ struct Ws {
   int* ge0;              // [ngal + 1] first edge
   int* gr0;              // [ngal + 1] first flux row
   PRec* rec;             // [n]
+  TcPar* tpar;           // [n] tensor-core forms only (else null)
   int* npairs;           // [n] tiles touched per particle
   long long* pair_off;   // [n] exclusive scan of npairs
   int* tile_count;       // [ntiles]

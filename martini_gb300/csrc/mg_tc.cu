@@ -110,12 +110,14 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
                : "memory");
 }
-// one particle record (72 bytes: nine 8-byte pieces)
-__device__ __forceinline__ void cp_async_rec(void* dst, const void* src) {
-  static_assert(sizeof(PRec) % 8 == 0, "records copy in 8-byte pieces");
+// one TcPar (64 bytes: four 16-byte pieces; both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async_tpar(void* dst, const void* src) {
 #pragma unroll
-  for (int k = 0; k < (int)(sizeof(PRec) / 8); ++k)
-    cp_async8(static_cast<char*>(dst) + 8 * k, static_cast<const char*>(src) + 8 * k);
+  for (int k = 0; k < 4; ++k)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     smem_u32(static_cast<char*>(dst) + 16 * k)),
+                 "l"(static_cast<const char*>(src) + 16 * k)
+                 : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
@@ -246,6 +248,19 @@ __device__ __forceinline__ void split2(float v, unsigned short& hi, unsigned sho
     hi = __half_as_ushort(h);
     lo = __half_as_ushort(__float2half_rn(v - __half2float(h)));
   }
+}
+
+__device__ __forceinline__ TcPar empty_tpar() {
+  TcPar z;
+  z.xi = z.yi = 0;
+  z.xf = z.yf = z.k2 = z.scale = 0.f;
+  z.kind = 0;
+  z.clo = 1;
+  z.chi = 0;
+  z.ilo = 0; z.ihi = -1; z.jlo = 0; z.jhi = -1;
+  z.pad_ = 0;
+  z.soff = 0;
+  return z;
 }
 
 struct ItemTC {
@@ -640,12 +655,12 @@ struct SPar {
   unsigned n;      // support channels in the row; 0: contributes nothing
 };
 
-// StagePar / SPar of one particle of a stage (valid: listed for this stage;
-// the record of an unused slot is empty).  Returns the WK_* kind and flags.
-__device__ __forceinline__ int build_par(const PRec& r, bool valid, int i0, int j0, int cb0,
-                                         int cb1, const KSpec* ks, int ktab_type, float sw,
-                                         StagePar& P, SPar& S) {
-  valid = valid && r.ilo <= r.ihi && r.jlo <= r.jhi && r.chi >= cb0 && r.clo <= cb1;
+// The tile-independent parameters of one particle (k_tc_params): kernel
+// kind and constants with the cube's operand scale sw, position, box,
+// support.  A particle that reaches no pixel or no channel gets kind 0.
+__device__ __forceinline__ TcPar tc_param(const PRec& r, const KSpec* ks, int ktab_type, float sw,
+                                          long long soff) {
+  const bool valid = r.ilo <= r.ihi && r.jlo <= r.jhi && r.clo <= r.chi;
   const KSpec kk = ks[r.kslot];
   const int t = kk.type;
   int kind = WK_NONE;
@@ -671,18 +686,45 @@ __device__ __forceinline__ int build_par(const PRec& r, bool valid, int i0, int 
       if ((r.flags & PREC_ROWS_COVER) && (r.flags & PREC_COLS_COVER)) kind |= WK_COVER;
     }
   }
-  P.dxr = (float)(r.xi - i0);
-  P.xf = r.xf;
-  P.dyr = (float)(r.yi - j0);
-  P.yf = r.yf;
-  P.k2 = k2;
-  P.scale = scale;
-  P.kind = kind | (r.kslot << 8) | (t << 12);
+  TcPar q;
+  q.xi = r.xi;
+  q.yi = r.yi;
+  q.xf = r.xf;
+  q.yf = r.yf;
+  q.k2 = k2;
+  q.scale = scale;
+  q.kind = kind == WK_NONE ? 0 : (kind | (r.kslot << 8) | (t << 12));
+  q.clo = r.clo;
+  q.ilo = r.ilo;
+  q.ihi = r.ihi;
+  q.jlo = r.jlo;
+  q.jhi = r.jhi;
+  q.chi = r.chi;
+  q.pad_ = 0;
+  q.soff = soff;
+  return q;
+}
+
+// StagePar / SPar of one particle of a stage, tile-relative (listed: in this
+// stage; a particle whose line misses the segment's block contributes
+// nothing).  Returns the WK_* kind and flags.
+__device__ __forceinline__ int build_stage(const TcPar& t, bool listed, int i0, int j0, int cb0,
+                                           int cb1, StagePar& P, SPar& S) {
+  const bool valid = listed && t.kind != 0 && t.chi >= cb0 && t.clo <= cb1;
+  const int kind = valid ? t.kind : 0;
+  P.dxr = (float)(t.xi - i0);
+  P.xf = t.xf;
+  P.dyr = (float)(t.yi - j0);
+  P.yf = t.yf;
+  // an empty slot: zero k2 and scale (u = 0 and a zero weight in every path)
+  P.k2 = valid ? t.k2 : 0.f;
+  P.scale = valid ? t.scale : 0.f;
+  P.kind = kind;
   // box rows / columns within the tile as bit masks
   unsigned rows = 0u, cols = 0u;
-  if (kind != WK_NONE) {
-    const int a = max(r.ilo - i0, 0), b = min(r.ihi - i0, TILE_I - 1);
-    const int c = max(r.jlo - j0, 0), d = min(r.jhi - j0, TILE_J - 1);
+  if (valid) {
+    const int a = max(t.ilo - i0, 0), b = min(t.ihi - i0, TILE_I - 1);
+    const int c = max(t.jlo - j0, 0), d = min(t.jhi - j0, TILE_J - 1);
     if (a <= b) rows = ((2u << b) - 1u) & ~((1u << a) - 1u);
     if (c <= d) cols = ((2u << d) - 1u) & ~((1u << c) - 1u);
     if (kind & WK_COVER) {
@@ -692,8 +734,9 @@ __device__ __forceinline__ int build_par(const PRec& r, bool valid, int i0, int 
     }
   }
   P.mask = (int)(rows | cols << 8);
-  S.clo = r.clo;
-  S.n = (valid && r.chi >= r.clo) ? (unsigned)(r.chi - r.clo + 1) : 0u;
+  S.soff = t.soff;
+  S.clo = t.clo;
+  S.n = valid ? (unsigned)(t.chi - t.clo + 1) : 0u;
   return kind;
 }
 
@@ -987,7 +1030,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   constexpr int DRAIN_STAGES = NP == 3 ? 1 : TC_DRAIN;
   constexpr int KSTEPS = KC / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(16) PRec recs[2][KC];
+  __shared__ __align__(16) TcPar s_tp[2][KC];  // the stage's particles (cp.async targets)
   __shared__ int s_pid[2][KC];
   __shared__ int2 s_lohi[2][KC];   // support [clo, chi] of each listed particle (window)
   __shared__ __align__(16) StagePar s_par[2][KC];  // weight producers' view of a stage
@@ -1133,21 +1176,17 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     const int cb0 = it.c0, cb1 = it.c0 + ncols - 1;  // the segment's channel block
     if (rec_lane) {
       const bool listed = rq < it.lcount;
+      TcPar t = empty_tpar();
       if (listed) {
         const int pid = w.list[it.lbeg + rq];
-        recs[0][rq] = w.rec[pid];
+        t = w.tpar[pid];
         s_pid[0][rq] = pid;
-        s_spar[0][rq].soff = spec ? w.pair_off[pid] : 0;
       } else {
-        recs[0][rq] = empty_rec();
         s_pid[0][rq] = 0;
-        s_spar[0][rq].soff = 0;
       }
       if (KC + rq < it.lcount) pid_ahead = w.list[it.lbeg + KC + rq];
-      const PRec& r = recs[0][rq];
-      s_lohi[0][rq] = listed ? make_int2(r.clo, r.chi) : make_int2(0x7fffffff, -1);
-      s_kind[0][rq] = build_par(r, listed, i0, j0, cb0, cb1, s_ks, ktab_type, sw, s_par[0][rq],
-                                s_spar[0][rq]);
+      s_lohi[0][rq] = listed ? make_int2(t.clo, t.chi) : make_int2(0x7fffffff, -1);
+      s_kind[0][rq] = build_stage(t, listed, i0, j0, cb0, cb1, s_par[0][rq], s_spar[0][rq]);
     }
     __syncthreads();
 
@@ -1168,14 +1207,11 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (has_next && rec_lane) {
         if (k0 + KC + rq < it.lcount) {
           const int npid = pid_ahead;
-          cp_async_rec(&recs[buf ^ 1][rq], w.rec + npid);
-          if (spec) cp_async8(&s_spar[buf ^ 1][rq].soff, w.pair_off + npid);
-          else s_spar[buf ^ 1][rq].soff = 0;
+          cp_async_tpar(&s_tp[buf ^ 1][rq], w.tpar + npid);
           s_pid[buf ^ 1][rq] = npid;
         } else {
-          recs[buf ^ 1][rq] = empty_rec();
+          s_tp[buf ^ 1][rq] = empty_tpar();
           s_pid[buf ^ 1][rq] = 0;
-          s_spar[buf ^ 1][rq].soff = 0;
         }
         cp_async_commit();
         if (k0 + 2 * KC + rq < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + rq];
@@ -1251,8 +1287,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
 #pragma unroll
         for (int pp = 0; pp < PPW; pp += 2) {
           const int q = warp * PPW + pp;
-          const PRec r0 = recs[buf][q];
-          const PRec r1 = recs[buf][q + 1];
+          const PRec r0 = q < kn ? w.rec[s_pid[buf][q]] : empty_rec();
+          const PRec r1 = q + 1 < kn ? w.rec[s_pid[buf][q + 1]] : empty_rec();
           // a particle listed for this block whose line misses the block
           // (the list bound is conservative) contributes nothing
           const bool v0 = q < kn && r0.chi >= cb0 && r0.clo <= cb1;
@@ -1266,10 +1302,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (has_next && rec_lane) {
         cp_async_wait_all();
         const bool listed = k0 + KC + rq < it.lcount;
-        const PRec& r = recs[buf ^ 1][rq];
-        s_lohi[buf ^ 1][rq] = listed ? make_int2(r.clo, r.chi) : make_int2(0x7fffffff, -1);
-        s_kind[buf ^ 1][rq] = build_par(r, listed, i0, j0, cb0, cb1, s_ks, ktab_type, sw,
-                                        s_par[buf ^ 1][rq], s_spar[buf ^ 1][rq]);
+        const TcPar& t = s_tp[buf ^ 1][rq];
+        s_lohi[buf ^ 1][rq] = listed ? make_int2(t.clo, t.chi) : make_int2(0x7fffffff, -1);
+        s_kind[buf ^ 1][rq] = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][rq],
+                                          s_spar[buf ^ 1][rq]);
       }
       fence_proxy_async();
       __syncthreads();
@@ -1468,9 +1504,45 @@ void launch_spec_store(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
   k_spec_eval<<<eblocks, 256, 0, s>>>(g, w);
 }
 
+// The tensor-core producers' per-particle parameters (TcPar), once per
+// insertion: the launch's radial kernel type (its table sits in shared
+// memory in the contraction), each cube's operand scale sw, the spectrum-
+// store row (pair_off holds the store's row offsets after the SPEC stage).
+__global__ void k_tc_params(Geo g, Ws w) {
+  __shared__ KSpec s_ks[MG_MAX_KERNELS];
+  if (threadIdx.x < MG_MAX_KERNELS) s_ks[threadIdx.x] = g.ks[threadIdx.x];
+  __syncthreads();
+  int ktab_type = -1;
+  for (int k = 0; k < g.n_kernels; ++k)
+    if (g.ks[k].type <= MG_KERNEL_QUARTIC_SPLINE) ktab_type = g.ks[k].type;
+  if (ktab_type >= 0 && kt_info[ktab_type].ncoef > KT_SMEM_CELLS) ktab_type = -1;
+  const bool f16 = g.form == MG_FORM_F16X3;
+  int gk = -1;
+  long long gp1 = -1;
+  float sw = 1.f;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (gk < 0 || p >= gp1) {
+      gk = find_gal(w.gp0, g.ngal, p);
+      gp1 = w.gp0[gk + 1];
+      sw = 1.f;
+      if (f16) {
+        const float wb = __uint_as_float(w.gst[gk].wbound_bits);
+        if (wb > 0.f) sw = exp2f(14.f - ceilf(log2f(wb)));
+      }
+    }
+    w.tpar[p] = tc_param(w.rec[p], s_ks, ktab_type, sw, w.pair_off[p]);
+  }
+}
+
 int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t s) {
   const int nwmax = g.max_width;  // a stage window never exceeds the widest block
   if (nwmax > TC_MASTER_COL) return MG_ERR_UNSUPPORTED;
+  if (g.n > 0) {
+    const unsigned blocks =
+        (unsigned)std::min<long long>((g.n + 255) / 256, (long long)num_sms * 16);
+    k_tc_params<<<blocks, 256, 0, s>>>(g, w);
+  }
   // stage size: the form's default unless the launch shape asks for 32
   const bool kc32 = g.kc == 32;
   int rc;
