@@ -745,17 +745,6 @@ constexpr int GP_GENERAL = 0;  // each particle takes its kind's path
 constexpr int GP_MIXED = 1;    // table / Dirac / empty: one branch-free block with box tests
 constexpr int GP_COVERED = 2;  // table kernels whose boxes hold their supports, or empty
 
-// The path of an 8-particle group from its particles' kinds (called by a
-// whole warp; lane l looks at particle l % 8).
-__device__ __forceinline__ int group_path(const int* kinds, int lane) {
-  const int kind = kinds[lane & 7];
-  const int k = kind & 7;
-  const bool covered = k == WK_NONE || (k == WK_TAB && (kind & WK_COVER));
-  const bool mixed = k == WK_NONE || k == WK_TAB || k == WK_DIRAC;
-  if (__all_sync(0xffffffffu, covered)) return GP_COVERED;
-  return __all_sync(0xffffffffu, mixed) ? GP_MIXED : GP_GENERAL;
-}
-
 __device__ __forceinline__ float horner3(const float4& cf, float t) {
   return fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
 }
@@ -995,22 +984,25 @@ __device__ __forceinline__ void s_task_store(const unsigned (&v)[8], int g8, int
   }
 }
 
-// Min clo and max chi over a stage's KC particles (listed slots; others
-// hold an empty range), reduced by a whole warp.
-template <int KC>
-__device__ __forceinline__ int2 stage_window(const int2* lohi, int lane) {
-  int2 v = lohi[lane];
-  if (KC > 32) {
-    const int2 u = lohi[lane + 32];
-    v.x = min(v.x, u.x);
-    v.y = max(v.y, u.y);
-  }
+// What a build warp tells the others about its 32 particles of a stage:
+// the union of their supports and the path of each of its 8-particle groups.
+// Lane l holds particle l (kind 0 for an empty slot).
+__device__ __forceinline__ void build_summary(int clo, int chi, int kind, int lane, int2* win,
+                                              int* gp) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    v.x = min(v.x, __shfl_xor_sync(0xffffffffu, v.x, o));
-    v.y = max(v.y, __shfl_xor_sync(0xffffffffu, v.y, o));
+    clo = min(clo, __shfl_xor_sync(0xffffffffu, clo, o));
+    chi = max(chi, __shfl_xor_sync(0xffffffffu, chi, o));
   }
-  return v;
+  const int k = kind & 7;
+  const unsigned cov =
+      __ballot_sync(0xffffffffu, k == WK_NONE || (k == WK_TAB && (kind & WK_COVER)));
+  const unsigned mix = __ballot_sync(0xffffffffu, k == WK_NONE || k == WK_TAB || k == WK_DIRAC);
+  if (lane == 0) *win = make_int2(clo, chi);
+  if (lane < 4) {
+    const unsigned c8 = (cov >> (8 * lane)) & 0xffu, m8 = (mix >> (8 * lane)) & 0xffu;
+    gp[lane] = c8 == 0xffu ? GP_COVERED : (m8 == 0xffu ? GP_MIXED : GP_GENERAL);
+  }
 }
 
 template <int SPLIT, int KC>
@@ -1018,13 +1010,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
   static_assert(KC == split_kc(SPLIT) || (KC == 32 && split_parts(SPLIT) == 2),
                 "stage size of the split");
-  static_assert(KC == 32 || KC == 64, "records of a stage: KC / 16 lanes of every warp");
+  static_assert(KC == 32 || KC == 64, "records of a stage: one per lane of KC / 32 warps");
   constexpr bool BF16 = split_bf16(SPLIT);
   constexpr int NP = split_parts(SPLIT);  // 16-bit pieces per operand
-  // A stage's records are handled by the first RPW lanes of every warp (record
-  // slot rq = warp * RPW + lane), so that copying them and turning them into
-  // parameters adds the same few instructions to every warp.
-  constexpr int RPW = KC / (TC_THREADS / 32);
+  // Roles of the warps in a stage.  Every warp computes one weight task.
+  // The last NB = KC / 32 warps (build warps) also copy the next stage's
+  // particle parameters and turn them into stage parameters, one particle
+  // per lane (slot bq); lane 0 of the warp before them issues the MMAs
+  // after the stage barrier; the other NSW warps take the spectrum tasks.
+  constexpr int NWARP = TC_THREADS / 32;
+  constexpr int NB = KC / 32;
+  constexpr int MMA_WARP = NWARP - NB - 1;
+  constexpr int NSW = MMA_WARP;
   // stages between drains: TC_DRAIN for pairs (24 MMAs), every stage for
   // three pieces (the same 24 MMAs, over half the particles)
   constexpr int DRAIN_STAGES = NP == 3 ? 1 : TC_DRAIN;
@@ -1032,10 +1029,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(16) TcPar s_tp[2][KC];  // the stage's particles (cp.async targets)
   __shared__ int s_pid[2][KC];
-  __shared__ int2 s_lohi[2][KC];   // support [clo, chi] of each listed particle (window)
+  __shared__ int2 s_win[2][NB];    // support union [clo, chi] per build warp (window)
+  __shared__ int s_gp[2][KC / 8];  // path of each 8-particle group (GP_*)
   __shared__ __align__(16) StagePar s_par[2][KC];  // weight producers' view of a stage
   __shared__ __align__(16) SPar s_spar[2][KC];     // spectrum producers' view
-  __shared__ int s_kind[2][KC];    // WK_* kind and flags of each particle
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
   __shared__ __align__(8) unsigned long long bars[2];
@@ -1045,8 +1042,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const bool rec_lane = lane < RPW;  // this thread handles record slot rq
-  const int rq = warp * RPW + lane;
+  const bool bld = warp >= NWARP - NB;         // a build warp
+  const int bq = (warp - (NWARP - NB)) * 32 + lane;  // its particle slot
   if (w.hdr->status) return;
   const long long n_items = w.hdr->n_items;
   const int kch = w.hdr->kch;
@@ -1174,19 +1171,20 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     // records of the first stage; the list entry of the second
     int pid_ahead = 0;
     const int cb0 = it.c0, cb1 = it.c0 + ncols - 1;  // the segment's channel block
-    if (rec_lane) {
-      const bool listed = rq < it.lcount;
+    if (bld) {
+      const bool listed = bq < it.lcount;
       TcPar t = empty_tpar();
       if (listed) {
-        const int pid = w.list[it.lbeg + rq];
+        const int pid = w.list[it.lbeg + bq];
         t = w.tpar[pid];
-        s_pid[0][rq] = pid;
+        s_pid[0][bq] = pid;
       } else {
-        s_pid[0][rq] = 0;
+        s_pid[0][bq] = 0;
       }
-      if (KC + rq < it.lcount) pid_ahead = w.list[it.lbeg + KC + rq];
-      s_lohi[0][rq] = listed ? make_int2(t.clo, t.chi) : make_int2(0x7fffffff, -1);
-      s_kind[0][rq] = build_stage(t, listed, i0, j0, cb0, cb1, s_par[0][rq], s_spar[0][rq]);
+      if (KC + bq < it.lcount) pid_ahead = w.list[it.lbeg + KC + bq];
+      const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[0][bq], s_spar[0][bq]);
+      build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
+                    &s_win[0][bq >> 5], &s_gp[0][(bq >> 5) * 4]);
     }
     __syncthreads();
 
@@ -1204,23 +1202,27 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       // this one is produced (its list entry was read a stage earlier); the
       // list entry of the stage after is read now
       const bool has_next = ch + 1 < nchunk;
-      if (has_next && rec_lane) {
-        if (k0 + KC + rq < it.lcount) {
+      if (has_next && bld) {
+        if (k0 + KC + bq < it.lcount) {
           const int npid = pid_ahead;
-          cp_async_tpar(&s_tp[buf ^ 1][rq], w.tpar + npid);
-          s_pid[buf ^ 1][rq] = npid;
+          cp_async_tpar(&s_tp[buf ^ 1][bq], w.tpar + npid);
+          s_pid[buf ^ 1][bq] = npid;
         } else {
-          s_tp[buf ^ 1][rq] = empty_tpar();
-          s_pid[buf ^ 1][rq] = 0;
+          s_tp[buf ^ 1][bq] = empty_tpar();
+          s_pid[buf ^ 1][bq] = 0;
         }
         cp_async_commit();
-        if (k0 + 2 * KC + rq < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + rq];
+        if (k0 + 2 * KC + bq < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + bq];
       }
       // stage channel window [w0, w0 + nw): min clo, max chi
       int w0, nw;
       {
         // the extremes of the stage's listed particles' supports
-        const int2 lh = stage_window<KC>(s_lohi[buf], lane);
+        int2 lh = s_win[buf][0];
+        if (NB > 1) {
+          const int2 u = s_win[buf][NB - 1];
+          lh = make_int2(min(lh.x, u.x), max(lh.y, u.y));
+        }
         int lo = lh.x, hi = lh.y;
         // relative to the segment's block [c0, c0 + ncols)
         lo = max(lo, it.c0) - it.c0;
@@ -1255,19 +1257,16 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       constexpr int PXL = KC / 32;  // pixels per lane
       constexpr int NG8 = KC / 8;   // particle groups of a stage
       const int wa = it.c0 + w0;    // first window channel (absolute)
-      // spectrum tasks go round robin over the warps; the loads of a warp's
-      // first task are in flight during its weights
+      // spectrum tasks go round robin over the first NSW warps; the loads of
+      // a warp's first task are in flight during its weights
       const int n_chunks = (nw + 31) >> 5;
       const int n_stasks = spec ? n_chunks * NG8 : 0;
-      constexpr int NWARP = TC_THREADS / 32;
-      const int t0 = warp;
+      const int t0 = warp < NSW ? warp : n_stasks;
       unsigned sv[8];
       if (t0 < n_stasks)
         s_task_load(s_spar[buf] + 8 * (t0 % NG8), spec, wa, 32 * (t0 / NG8) + lane, sv);
       produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8),
-                                 ktab_type >= 0 ? group_path(s_kind[buf] + 8 * (warp % NG8), lane)
-                                                : GP_GENERAL,
-                                 s_ks,
+                                 ktab_type >= 0 ? s_gp[buf][warp % NG8] : GP_GENERAL, s_ks,
                                  smem_u32(s_ktab), ucap, warp % NG8, warp / NG8, lane, sa, a_bytes);
       // the drain of the previous interval: its MMAs are done by now
       if (drain_due) drain_now();  // block-uniform
@@ -1275,7 +1274,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (spec) {
         // Gaussian lines from the spectrum store: tasks of (32-channel
         // chunk, 8-particle group), round robin over the warps
-        for (int t = t0; t < n_stasks; t += NWARP) {
+        for (int t = t0; t < n_stasks; t += NSW) {
           const int g8 = t % NG8, n = 32 * (t / NG8) + lane;
           if (t != t0) s_task_load(s_spar[buf] + 8 * g8, spec, wa, n, sv);
           if (n < nw) s_task_store<SPLIT>(sv, g8, n, nw, sb, b_bytes);
@@ -1299,18 +1298,19 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
                                 lane, ss, sb, b_bytes);
         }
       }
-      if (has_next && rec_lane) {
+      if (has_next && bld) {
         cp_async_wait_all();
-        const bool listed = k0 + KC + rq < it.lcount;
-        const TcPar& t = s_tp[buf ^ 1][rq];
-        s_lohi[buf ^ 1][rq] = listed ? make_int2(t.clo, t.chi) : make_int2(0x7fffffff, -1);
-        s_kind[buf ^ 1][rq] = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][rq],
-                                          s_spar[buf ^ 1][rq]);
+        const bool listed = k0 + KC + bq < it.lcount;
+        const TcPar& t = s_tp[buf ^ 1][bq];
+        const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][bq],
+                                     s_spar[buf ^ 1][bq]);
+        build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
+                      &s_win[buf ^ 1][bq >> 5], &s_gp[buf ^ 1][(bq >> 5) * 4]);
       }
       fence_proxy_async();
       __syncthreads();
       if (s_abort) break;
-      if (tid == 0) {
+      if (tid == MMA_WARP * 32) {
         tc_fence_after();
         // nw <= nwmax <= 256: one MMA spans the window.  The descriptors'
         // start-address field (bits 0-13, address / 16) steps by adding the
