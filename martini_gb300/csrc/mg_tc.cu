@@ -229,6 +229,15 @@ __device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16
       : "memory");
 }
 
+__device__ __forceinline__ void tmem_st16_zero(unsigned taddr) {
+  const unsigned z = 0u;
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+      "%1, %1, %1, %1, %1, %1};" ::"r"(taddr),
+      "r"(z)
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -1111,18 +1120,21 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   };
   // master += working (round to nearest), working = 0 over the columns
   // written since the last drain; no MMA in flight
+  // The drain of columns [lo, hi): the four warps of a lane quarter take its
+  // 16-column pieces round robin, so every warp drains about a quarter of
+  // the interval (a column past what the MMAs wrote is zero and adds
+  // nothing).
   auto drain_tmem = [&](int lo, int hi) {
-    for (int c = colgrp * 32; c < ncols; c += 128) {
-      if (!chunk_in(c, lo, hi)) continue;
-      unsigned a[32], b[32];
-      tmem_ld32(tmem + lane_base + c, a);
-      tmem_ld32(tmem + lane_base + TC_MASTER_COL + c, b);
+    for (int c = (lo & ~15) + 16 * colgrp; c < hi; c += 64) {
+      unsigned a[16], b[16];
+      tmem_ld16(tmem + lane_base + c, a);
+      tmem_ld16(tmem + lane_base + TC_MASTER_COL + c, b);
       tmem_wait_ld();
 #pragma unroll
-      for (int v = 0; v < 32; ++v)
+      for (int v = 0; v < 16; ++v)
         b[v] = __float_as_uint(__uint_as_float(a[v]) + __uint_as_float(b[v]));
-      tmem_st32(tmem + lane_base + TC_MASTER_COL + c, b);
-      tmem_st32_zero(tmem + lane_base + c);
+      tmem_st16(tmem + lane_base + TC_MASTER_COL + c, b);
+      tmem_st16_zero(tmem + lane_base + c);
     }
     tmem_wait_st();
   };
