@@ -332,8 +332,8 @@ int make_batch(const mg_problem* probs, int nprob, Batch* b, bool shape_only = f
   g.nedge = nedge;
   g.nrows = (int)nrows;
   g.nfpart = nfpart;
-  // sort-key bits below the segment: a kernel-class bit above the channel
-  g.cbits = channel_bits(g.max_nc) + 1;
+  // sort-key bits below the segment: two kernel-class bits above the channel
+  g.cbits = channel_bits(g.max_nc) + 2;
   return MG_OK;
 }
 

@@ -377,10 +377,10 @@ __device__ __forceinline__ int div_exact(int a, int b, float rb) {
 }
 
 // Pairs in particle order: key = global segment << cbits | class << (cbits -
-// 1) | clo, class = 1 for the Gaussian and cubic-spline kernels (their
-// particles then form stages of their own, after the table and Dirac
-// kernels' in each segment; the tensor-core producers take such stages on a
-// separate path) (one pair per
+// 2) | clo, class 0 for the table kernels, 1 for the Dirac kernel, 2 for the
+// Gaussian and cubic-spline kernels (each class's particles then form
+// stages of their own in each segment, which the tensor-core producers take
+// on the class's own path) (one pair per
 // tile and channel block the particle's line meets), value = particle.  A
 // warp takes 32 particles, whose pairs are one contiguous range of the
 // output (pair_off is the exclusive scan of the counts); each lane writes
@@ -414,7 +414,9 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
         nb = G.ncb > 1 ? rec.chi / G.width - cb0 + 1 : 1;
         clo = rec.clo;
         const int kt = g.ks[rec.kslot].type;
-        cls = (kt == MG_KERNEL_GAUSSIAN || kt == MG_KERNEL_CUBIC_SPLINE) ? 1u : 0u;
+        cls = (kt == MG_KERNEL_GAUSSIAN || kt == MG_KERNEL_CUBIC_SPLINE) ? 2u
+              : kt == MG_KERNEL_DIRAC                                     ? 1u
+                                                                          : 0u;
         seg0 = G.seg0;
         nty = G.nty;
         ncb = G.ncb;
@@ -454,7 +456,7 @@ __global__ void k_emit(Geo g, Ws w, unsigned* __restrict__ keys, int* __restrict
         const int a = div_exact(t, sspan, __frcp_rn((float)sspan));
         const int tx = stx0 + a, ty = sty0 + (t - a * sspan);
         const unsigned sg = (unsigned)(sseg0 + (tx * snty + ty) * sncb + cb);
-        keys[f] = (sg << g.cbits) | (scls << (g.cbits - 1)) | (unsigned)sclo;
+        keys[f] = (sg << g.cbits) | (scls << (g.cbits - 2)) | (unsigned)sclo;
         vals[f] = (int)(base + src);
       }
     }

@@ -143,8 +143,8 @@ struct Geo {
   int nseg;           // segments of all cubes
   int max_width;      // widest channel block (partial slots hold TILE_PX x max_width)
   int max_nc;
-  int cbits;          // key bits below the segment: a kernel-class bit, then the channel
-                      // bits of the widest band
+  int cbits;          // key bits below the segment: two kernel-class bits, then the
+                      // channel bits of the widest band
   int nrows;          // flux rows of all cubes
   int max_diff;       // largest difference array of one cube
   long long n;        // particles of all cubes

@@ -753,16 +753,41 @@ __device__ __forceinline__ int build_stage(const TcPar& t, bool listed, int i0, 
 constexpr int GP_GENERAL = 0;  // each particle takes its kind's path
 constexpr int GP_MIXED = 1;    // table / Dirac / empty: one branch-free block with box tests
 constexpr int GP_COVERED = 2;  // table kernels whose boxes hold their supports, or empty
+constexpr int GP_GAUSS = 3;    // Gaussian kernels or empty: one branch-free block
+constexpr int GP_DIRAC = 4;    // Dirac kernels or empty: the box test picks the scale
 
 __device__ __forceinline__ float horner3(const float4& cf, float t) {
   return fmaf(fmaf(fmaf(cf.w, t, cf.z), t, cf.y), t, cf.x);
+}
+
+// GaussianKernel pixel integral (sph_kernels.py:994-1044):
+// 0.25 erf(zmax / sqrt 2) (erf(x1) - erf(x0)) (erf(y1) - erf(y0)) / norm.
+// gauss_factor: the erf difference of lane's line of pixels -- column `lane`
+// for lanes 0-15, row wr0 + (lane - 16) mod 2 PXL for lanes 16 and up -- to
+// be shared by shuffles (an empty slot, k2 = 0, gives 0).
+template <int PXL>
+__device__ __forceinline__ float gauss_factor(const StagePar& P, int wr0, int lane) {
+  const float sc = P.k2 * 0.70710678118654752f;  // 1 / (h sqrt(2) sigma)
+  const float d = lane < 16 ? (P.dyr - (float)lane) + P.yf
+                            : (P.dxr - (float)(wr0 + ((lane - 16) & (2 * PXL - 1)))) + P.xf;
+  return erff((d + 0.5f) * sc) - erff((d - 0.5f) * sc);
+}
+// The truncation factor erf(zmax / sqrt 2) at squared offset q2 (pixel units)
+// from its cubic cells in zmax, in shared memory at gtab_s32 (minus 2^23
+// cells, as kt_cell_smem takes it); t2 = truncate^2, ihs2 = 1 / (h sigma)^2.
+__device__ __forceinline__ float gauss_trunc(unsigned gtab_s32, float q2, float ihs2, float t2) {
+  const float z2 = fmaxf(fmaf(-q2, ihs2, t2), 0.f);  // truncate^2 - q^2
+  const float u = fminf(sqrt_approx(z2) * GT_CELLS_PER_UNIT, (float)GT_NCELL);
+  float t;
+  const float4 cf = kt_cell_smem(gtab_s32, u, t);
+  return horner3(cf, t);
 }
 
 // Weights of one stage particle at a lane's PXL pixels (tile rows il[k],
 // column jl).  Warp-uniform: every lane takes the same branch.
 template <int PXL>
 __device__ __forceinline__ void w_particle(const StagePar& P, const KSpec* ks, unsigned ktab_s32,
-                                           float ucap, int wr0, const int (&il)[PXL],
+                                           unsigned gtab_s32, float ucap, int wr0, const int (&il)[PXL],
                                            const float (&ilf)[PXL], int jl, float jlf, int lane,
                                            float (&w)[PXL]) {
 #pragma unroll
@@ -796,31 +821,19 @@ __device__ __forceinline__ void w_particle(const StagePar& P, const KSpec* ks, u
     return;
   }
   if (kind == WK_GAUSS) {
-    // GaussianKernel pixel integral (sph_kernels.py:994-1044):
-    // 0.25 erf(zmax / sqrt 2) (erf(x1) - erf(x0)) (erf(y1) - erf(y0)) / norm.
-    // Column factors from lanes 0-15, the warp's row factors from lanes
-    // 16 .. 16 + 2 PXL - 1 (two erff each), shared by shuffles; the
-    // truncation factor from its cubic cells in zmax.
-    const float inv_hs = P.k2;
-    const float sc = inv_hs * 0.70710678118654752f;  // 1 / (h sqrt(2) sigma)
-    const float d = lane < 16 ? (P.dyr - (float)lane) + P.yf
-                              : (P.dxr - (float)(wr0 + ((lane - 16) & (2 * PXL - 1)))) + P.xf;
-    const float e = erff((d + 0.5f) * sc) - erff((d - 0.5f) * sc);
+    // column factors from lanes 0-15, the warp's row factors from lanes
+    // 16 .. 16 + 2 PXL - 1, shared by shuffles
+    const float e = gauss_factor<PXL>(P, wr0, lane);
     const float ey = __shfl_sync(0xffffffffu, e, jl);
     const KSpec kk = ks[(P.kind >> 8) & 0xF];
     const float t2 = kk.truncate * kk.truncate;
-    const float ihs2 = inv_hs * inv_hs;
+    const float ihs2 = P.k2 * P.k2;
     const float dy2 = dy * dy;
     const float c = ey * P.scale;
-    const float4* gt = reinterpret_cast<const float4*>(gt_coef);
 #pragma unroll
     for (int k = 0; k < PXL; ++k) {
       const float ex = __shfl_sync(0xffffffffu, e, 16 + (il[k] - wr0));
-      const float z2 = fmaxf(fmaf(-fmaf(dx[k], dx[k], dy2), ihs2, t2), 0.f);  // truncate^2 - q^2
-      const float u = fminf(sqrt_approx(z2) * GT_CELLS_PER_UNIT, (float)GT_NCELL);
-      float t;
-      const int cell = kt_floor(u, t);
-      const float T = horner3(__ldg(gt + cell), t);
+      const float T = gauss_trunc(gtab_s32, fmaf(dx[k], dx[k], dy2), ihs2, t2);
       w[k] = in[k] ? T * ex * c : 0.f;
     }
     return;
@@ -888,10 +901,14 @@ __device__ __forceinline__ void store_row8(unsigned char* base, unsigned piece_b
 // chains with no box test (an empty slot has zero k2 and scale: u = 0 and a
 // zero weight).  GP_MIXED adds Dirac particles and box tests (an empty
 // slot's mask is empty, so u lands on the table's zero cell; DIRAC: the box
-// test picks sw).  GP_GENERAL: each particle takes its kind's path.
+// test picks sw).  GP_DIRAC: Dirac kernels (or empty), the box test alone.
+// GP_GAUSS: Gaussian kernels (or empty), their erf
+// factors as 8 independent chains.  GP_GENERAL: each particle takes its
+// kind's path.
 template <int SPLIT, int PXL>
 __device__ __forceinline__ void produce_w_task(const StagePar* par, int path, const KSpec* ks,
-                                               unsigned ktab_s32, float ucap, int g8, int pg,
+                                               unsigned ktab_s32, unsigned gtab_s32, float ucap,
+                                               int g8, int pg,
                                                int lane, unsigned char* a0, unsigned a_bytes) {
   const int jl = lane & 15;
   const float jlf = (float)jl;
@@ -943,10 +960,48 @@ __device__ __forceinline__ void produce_w_task(const StagePar* par, int path, co
         w[e][k] = dirac ? (in ? P.scale : 0.f) : wt;
       }
     }
+  } else if (path == GP_DIRAC) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const StagePar P = par[q];
+      const unsigned msk = (unsigned)P.mask;
+      const bool jin = (msk >> (8 + jl)) & 1u;
+#pragma unroll
+      for (int k = 0; k < PXL; ++k) w[q][k] = jin && ((msk >> il[k]) & 1u) ? P.scale : 0.f;
+    }
+  } else if (path == GP_GAUSS) {
+    // two particles' erf factors at a time (independent chains; more would
+    // spill registers), then their pixels' truncation factors and box tests
+#pragma unroll
+    for (int h = 0; h < 8; h += 2) {
+      float e[2];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) e[r] = gauss_factor<PXL>(par[h + r], wr0, lane);
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const StagePar P = par[h + r];
+        const unsigned msk = (unsigned)P.mask;
+        const bool jin = (msk >> (8 + jl)) & 1u;
+        const float ey = __shfl_sync(0xffffffffu, e[r], jl);
+        const float tr = ks[(P.kind >> 8) & 0xF].truncate;
+        const float ihs2 = P.k2 * P.k2;
+        const float dy = (P.dyr - jlf) + P.yf;
+        const float dy2 = dy * dy;
+        const float c = ey * P.scale;
+#pragma unroll
+        for (int k = 0; k < PXL; ++k) {
+          const float ex = __shfl_sync(0xffffffffu, e[r], 16 + (il[k] - wr0));
+          const float dx = (P.dxr - ilf[k]) + P.xf;
+          const float T = gauss_trunc(gtab_s32, fmaf(dx, dx, dy2), ihs2, tr * tr);
+          const bool in = jin && ((msk >> il[k]) & 1u);
+          w[h + r][k] = in ? T * ex * c : 0.f;
+        }
+      }
+    }
   } else {
 #pragma unroll
     for (int e = 0; e < 8; ++e)
-      w_particle<PXL>(par[e], ks, ktab_s32, ucap, wr0, il, ilf, jl, jlf, lane, w[e]);
+      w_particle<PXL>(par[e], ks, ktab_s32, gtab_s32, ucap, wr0, il, ilf, jl, jlf, lane, w[e]);
   }
   const unsigned goff = (unsigned)(g8 >> 1) * 4096u + (unsigned)(g8 & 1) * 128u;
 #pragma unroll
@@ -1007,10 +1062,17 @@ __device__ __forceinline__ void build_summary(int clo, int chi, int kind, int la
   const unsigned cov =
       __ballot_sync(0xffffffffu, k == WK_NONE || (k == WK_TAB && (kind & WK_COVER)));
   const unsigned mix = __ballot_sync(0xffffffffu, k == WK_NONE || k == WK_TAB || k == WK_DIRAC);
+  const unsigned gau = __ballot_sync(0xffffffffu, k == WK_NONE || k == WK_GAUSS);
+  const unsigned dir = __ballot_sync(0xffffffffu, k == WK_NONE || k == WK_DIRAC);
   if (lane == 0) *win = make_int2(clo, chi);
   if (lane < 4) {
     const unsigned c8 = (cov >> (8 * lane)) & 0xffu, m8 = (mix >> (8 * lane)) & 0xffu;
-    gp[lane] = c8 == 0xffu ? GP_COVERED : (m8 == 0xffu ? GP_MIXED : GP_GENERAL);
+    const unsigned g8 = (gau >> (8 * lane)) & 0xffu, d8 = (dir >> (8 * lane)) & 0xffu;
+    gp[lane] = d8 == 0xffu   ? GP_DIRAC
+               : c8 == 0xffu ? GP_COVERED
+               : m8 == 0xffu ? GP_MIXED
+               : g8 == 0xffu ? GP_GAUSS
+                             : GP_GENERAL;
   }
 }
 
@@ -1036,7 +1098,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   constexpr int DRAIN_STAGES = NP == 3 ? 1 : TC_DRAIN;
   constexpr int KSTEPS = KC / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(16) TcPar s_tp[2][KC];  // the stage's particles (cp.async targets)
+  // the next stage's particles (cp.async targets; only the build warps touch
+  // them, each its own slot: copied at a stage's start, read at its end)
+  __shared__ __align__(16) TcPar s_tp[KC];
   __shared__ int s_pid[2][KC];
   __shared__ int2 s_win[2][NB];    // support union [clo, chi] per build warp (window)
   __shared__ int s_gp[2][KC / 8];  // path of each 8-particle group (GP_*)
@@ -1044,6 +1108,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   __shared__ __align__(16) SPar s_spar[2][KC];     // spectrum producers' view
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
+  __shared__ float4 s_gtab[GT_NCELL + 1];  // Gaussian truncation cells
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
@@ -1082,6 +1147,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       ktab_type = -1;
     }
   }
+  for (int e = tid; e <= GT_NCELL; e += TC_THREADS)
+    s_gtab[e] = reinterpret_cast<const float4*>(gt_coef)[e];
+  const unsigned gtab_s32 = smem_u32(s_gtab) - (0x4B000000u << 4);
   // the zero cell past the support of the shared-memory table
   const float ucap = ktab_type >= 0 ? (float)kt_info[ktab_type].reg[0].ncell : 0.f;
   if (tid == 0) {
@@ -1120,12 +1188,14 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   };
   // master += working (round to nearest), working = 0 over the columns
   // written since the last drain; no MMA in flight
-  // The drain of columns [lo, hi): the four warps of a lane quarter take its
-  // 16-column pieces round robin, so every warp drains about a quarter of
-  // the interval (a column past what the MMAs wrote is zero and adds
-  // nothing).
+  // The drain of columns [lo, hi): the warps of a lane quarter take its
+  // 16-column pieces round robin (a column past what the MMAs wrote is zero
+  // and adds nothing).  A build warp (column group 3 of the last NB
+  // quarters) leaves its quarter's pieces to the other three.
+  const int dwarps = quarter >= 4 - NB ? 3 : 4;
   auto drain_tmem = [&](int lo, int hi) {
-    for (int c = (lo & ~15) + 16 * colgrp; c < hi; c += 64) {
+    if (colgrp >= dwarps) return;
+    for (int c = (lo & ~15) + 16 * colgrp; c < hi; c += 16 * dwarps) {
       unsigned a[16], b[16];
       tmem_ld16(tmem + lane_base + c, a);
       tmem_ld16(tmem + lane_base + TC_MASTER_COL + c, b);
@@ -1217,10 +1287,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (has_next && bld) {
         if (k0 + KC + bq < it.lcount) {
           const int npid = pid_ahead;
-          cp_async_tpar(&s_tp[buf ^ 1][bq], w.tpar + npid);
+          cp_async_tpar(&s_tp[bq], w.tpar + npid);
           s_pid[buf ^ 1][bq] = npid;
         } else {
-          s_tp[buf ^ 1][bq] = empty_tpar();
+          s_tp[bq] = empty_tpar();
           s_pid[buf ^ 1][bq] = 0;
         }
         cp_async_commit();
@@ -1269,24 +1339,31 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       constexpr int PXL = KC / 32;  // pixels per lane
       constexpr int NG8 = KC / 8;   // particle groups of a stage
       const int wa = it.c0 + w0;    // first window channel (absolute)
-      // spectrum tasks go round robin over the first NSW warps; the loads of
-      // a warp's first task are in flight during its weights
+      // Spectrum tasks: the first NSW go to warps 0 .. NSW - 1, the next
+      // NSW + 1 back from the MMA warp (NSW) to warp 0, so that a second task
+      // lands on the warps with the least other work first; the rest round
+      // robin over warps 0 .. NSW.  The loads of a warp's first task are in
+      // flight during its weights.
       const int n_chunks = (nw + 31) >> 5;
       const int n_stasks = spec ? n_chunks * NG8 : 0;
-      const int t0 = warp < NSW ? warp : n_stasks;
+      const int t0 = warp < NSW ? warp : (warp == NSW ? NSW : n_stasks);
       unsigned sv[8];
       if (t0 < n_stasks)
         s_task_load(s_spar[buf] + 8 * (t0 % NG8), spec, wa, 32 * (t0 / NG8) + lane, sv);
-      produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8),
-                                 ktab_type >= 0 ? s_gp[buf][warp % NG8] : GP_GENERAL, s_ks,
-                                 smem_u32(s_ktab), ucap, warp % NG8, warp / NG8, lane, sa, a_bytes);
+      // the table paths need the launch's table in shared memory
+      int path = s_gp[buf][warp % NG8];
+      if (ktab_type < 0 && (path == GP_COVERED || path == GP_MIXED)) path = GP_GENERAL;
+      produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8), path, s_ks,
+                                 smem_u32(s_ktab), gtab_s32, ucap, warp % NG8, warp / NG8, lane, sa,
+                                 a_bytes);
       // the drain of the previous interval: its MMAs are done by now
       if (drain_due) drain_now();  // block-uniform
       // ---- B = S
       if (spec) {
         // Gaussian lines from the spectrum store: tasks of (32-channel
         // chunk, 8-particle group), round robin over the warps
-        for (int t = t0; t < n_stasks; t += NSW) {
+        for (int t = t0; t < n_stasks;
+             t = t < NSW ? 2 * NSW - t : (t <= 2 * NSW ? 2 * NSW + 1 + warp : t + NSW + 1)) {
           const int g8 = t % NG8, n = 32 * (t / NG8) + lane;
           if (t != t0) s_task_load(s_spar[buf] + 8 * g8, spec, wa, n, sv);
           if (n < nw) s_task_store<SPLIT>(sv, g8, n, nw, sb, b_bytes);
@@ -1313,7 +1390,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (has_next && bld) {
         cp_async_wait_all();
         const bool listed = k0 + KC + bq < it.lcount;
-        const TcPar& t = s_tp[buf ^ 1][bq];
+        const TcPar& t = s_tp[bq];
         const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][bq],
                                      s_spar[buf ^ 1][bq]);
         build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
