@@ -215,7 +215,7 @@ int mg_insert_stages_batched(const mg_problem* probs, int32_t nprob, void* works
  */
 typedef struct mg_tuning {
   int32_t kc;            /* particles per tensor-core stage: 0 = the form's default
-                            (64 for pairs, 32 for bf16x6), or 32 (pair forms) */
+                            (64), or 32 (tensor-core forms) */
   int32_t items_per_sm;  /* work items per SM (split-K granularity), 1..24; 0 = 24 */
   int32_t cost_order;    /* 1: work queue ordered by estimated cost, largest first;
                             0: segment (tile) order */

@@ -37,17 +37,19 @@ bool known_form(int form) {
 }
 
 // Segment shape of a contraction form: channel blocks per tile and their
-// width.  Tensor-core forms: the band (rounded to 16) in one block up to 256
-// channels, else blocks of 256 (a block and its master accumulator fill the
-// 512 TMEM columns).
+// width.  Tensor-core forms: the band (rounded to 16) in one block up to the
+// form's block width, else blocks of that width: 256 for the pairs (a block
+// and its master accumulator fill the 512 TMEM columns), 128 for bf16x6
+// (two working accumulators and the master: its 64-particle stages).
 void seg_shape(int form, int nc, int* ncb, int* width) {
   if (form == MG_FORM_BF16X3 || form == MG_FORM_F16X3 || form == MG_FORM_BF16X6) {
-    if (nc <= 256) {
+    const int bw = form == MG_FORM_BF16X6 ? 128 : 256;
+    if (nc <= bw) {
       *ncb = 1;
       *width = (nc + 15) / 16 * 16;
     } else {
-      *ncb = (nc + 255) / 256;
-      *width = 256;
+      *ncb = (nc + bw - 1) / bw;
+      *width = bw;
     }
   } else {
     *ncb = (nc + CBLK - 1) / CBLK;
@@ -424,7 +426,6 @@ bool shape_ok(int form, const mg_tuning& t) {
   if (t.cost_order != 0 && t.cost_order != 1) return false;
   if (t.kc == 0) return true;
   if (form == MG_FORM_FP32) return false;
-  if (form == MG_FORM_BF16X6) return t.kc == 32;
   return t.kc == 32 || t.kc == 64;
 }
 
@@ -686,11 +687,11 @@ void mg_tuning_default(mg_tuning* out) {
 
 int mg_tuning_candidates(int32_t form, mg_tuning* out, int32_t cap) {
   std::vector<mg_tuning> c;
-  const bool pairs = form == MG_FORM_BF16X3 || form == MG_FORM_F16X3;
+  const bool tc = form == MG_FORM_BF16X3 || form == MG_FORM_F16X3 || form == MG_FORM_BF16X6;
   const int kcs[2] = {0, 32};
   const int ipss[2] = {ITEMS_PER_SM, ITEMS_PER_SM / 2};
   for (int kc : kcs) {
-    if (kc && !pairs) continue;
+    if (kc && !tc) continue;
     for (int ips : ipss)
       for (int order = 1; order >= 0; --order) {
         mg_tuning t;

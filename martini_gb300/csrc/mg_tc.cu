@@ -50,6 +50,11 @@ constexpr int TC_DRAIN = 2;
 // included: every table of mg_kernel_tables.h) are copied to shared memory.
 constexpr int KT_SMEM_CELLS = 1025;
 constexpr int TC_MASTER_COL = 256;
+// 64-particle stages of the three-piece split keep a second working
+// accumulator here (blocks of at most 128 channels): K-steps 0-1 accumulate
+// at column 0, K-steps 2-3 at this column, so each sees the MMA sequence of
+// a 32-particle stage before the drain
+constexpr int TC_WB_COL = 128;
 
 // Operand splits: a hi + lo pair of FP16 (scaled) or BF16 pieces, or three
 // BF16 pieces hi + mid + lo that represent the FP32 value exactly.
@@ -58,9 +63,8 @@ constexpr int SPLIT_BF16_2 = 1;
 constexpr int SPLIT_BF16_3 = 2;
 __host__ __device__ constexpr int split_parts(int split) { return split == SPLIT_BF16_3 ? 3 : 2; }
 __host__ __device__ constexpr bool split_bf16(int split) { return split != SPLIT_F16_2; }
-// default particles per stage: 64 for pairs, 32 for three pieces (the same
-// bytes); the pair forms also run with 32 (a launch-shape choice)
-__host__ __device__ constexpr int split_kc(int split) { return split == SPLIT_BF16_3 ? 32 : 64; }
+// Particles per stage: 64 by default, 32 as a launch-shape choice.  The
+// three-piece split's 64-particle stages fit with blocks of 128 channels.
 
 // Shared memory at the widest band: two stages of A and B pieces plus the
 // static arrays must fit in the 227 KB of a CTA.
@@ -77,6 +81,8 @@ static_assert(2 * tc_stage_bytes(SPLIT_F16_2, 64, TC_MASTER_COL) + tc_static_byt
 static_assert(2 * tc_stage_bytes(SPLIT_BF16_3, 32, TC_MASTER_COL) + tc_static_bytes(32) <=
                   227 * 1024,
               "tensor-core kernel shared memory (three pieces)");
+static_assert(2 * tc_stage_bytes(SPLIT_BF16_3, 64, TC_WB_COL) + tc_static_bytes(64) <= 227 * 1024,
+              "tensor-core kernel shared memory (three pieces, 64-particle stages)");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -110,12 +116,13 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
                : "memory");
 }
-// one TcPar (64 bytes: four 16-byte pieces; both addresses 16-byte aligned)
-__device__ __forceinline__ void cp_async_tpar(void* dst, const void* src) {
+// one TcPar (64 bytes: four 16-byte pieces), piece k to dst + k * stride
+// bytes (all addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async_tpar(void* dst, unsigned stride, const void* src) {
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                     smem_u32(static_cast<char*>(dst) + 16 * k)),
+                     smem_u32(dst) + k * stride),
                  "l"(static_cast<const char*>(src) + 16 * k)
                  : "memory");
 }
@@ -1053,11 +1060,8 @@ __device__ __forceinline__ void s_task_store(const unsigned (&v)[8], int g8, int
 // Lane l holds particle l (kind 0 for an empty slot).
 __device__ __forceinline__ void build_summary(int clo, int chi, int kind, int lane, int2* win,
                                               int* gp) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    clo = min(clo, __shfl_xor_sync(0xffffffffu, clo, o));
-    chi = max(chi, __shfl_xor_sync(0xffffffffu, chi, o));
-  }
+  clo = __reduce_min_sync(0xffffffffu, clo);
+  chi = __reduce_max_sync(0xffffffffu, chi);
   const int k = kind & 7;
   const unsigned cov =
       __ballot_sync(0xffffffffu, k == WK_NONE || (k == WK_TAB && (kind & WK_COVER)));
@@ -1079,8 +1083,7 @@ __device__ __forceinline__ void build_summary(int clo, int chi, int kind, int la
 template <int SPLIT, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_contract_tc(Geo g, Ws w, int nwmax) {
-  static_assert(KC == split_kc(SPLIT) || (KC == 32 && split_parts(SPLIT) == 2),
-                "stage size of the split");
+  static_assert(KC == 32 || KC == 64, "stage size");
   static_assert(KC == 32 || KC == 64, "records of a stage: one per lane of KC / 32 warps");
   constexpr bool BF16 = split_bf16(SPLIT);
   constexpr int NP = split_parts(SPLIT);  // 16-bit pieces per operand
@@ -1096,11 +1099,15 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   // stages between drains: TC_DRAIN for pairs (24 MMAs), every stage for
   // three pieces (the same 24 MMAs, over half the particles)
   constexpr int DRAIN_STAGES = NP == 3 ? 1 : TC_DRAIN;
+  // two working accumulators (K halves of a 64-particle stage, three pieces)
+  constexpr bool TWO_ACC = NP == 3 && KC == 64;
   constexpr int KSTEPS = KC / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
   // the next stage's particles (cp.async targets; only the build warps touch
-  // them, each its own slot: copied at a stage's start, read at its end)
-  __shared__ __align__(16) TcPar s_tp[KC];
+  // them, each its own slot: copied at a stage's start, read at its end),
+  // piece k of slot q at s_tp[k][q], so that a warp's 16-byte reads of one
+  // piece are contiguous
+  __shared__ __align__(16) uint4 s_tp[4][KC];
   __shared__ int s_pid[2][KC];
   __shared__ int2 s_win[2][NB];    // support union [clo, chi] per build warp (window)
   __shared__ int s_gp[2][KC / 8];  // path of each 8-particle group (GP_*)
@@ -1182,6 +1189,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     for (int c = colgrp * 32; c < ncols; c += 128) {
       if (!chunk_in(c, lo, hi)) continue;
       tmem_st32_zero(tmem + lane_base + c);
+      if (TWO_ACC) tmem_st32_zero(tmem + lane_base + TC_WB_COL + c);
       if (drain) tmem_st32_zero(tmem + lane_base + TC_MASTER_COL + c);
     }
     tmem_wait_st();
@@ -1199,7 +1207,17 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       unsigned a[16], b[16];
       tmem_ld16(tmem + lane_base + c, a);
       tmem_ld16(tmem + lane_base + TC_MASTER_COL + c, b);
-      tmem_wait_ld();
+      if constexpr (TWO_ACC) {
+        unsigned a2[16];
+        tmem_ld16(tmem + lane_base + TC_WB_COL + c, a2);
+        tmem_wait_ld();
+#pragma unroll
+        for (int v = 0; v < 16; ++v)
+          a[v] = __float_as_uint(__uint_as_float(a[v]) + __uint_as_float(a2[v]));
+        tmem_st16_zero(tmem + lane_base + TC_WB_COL + c);
+      } else {
+        tmem_wait_ld();
+      }
 #pragma unroll
       for (int v = 0; v < 16; ++v)
         b[v] = __float_as_uint(__uint_as_float(a[v]) + __uint_as_float(b[v]));
@@ -1287,10 +1305,12 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (has_next && bld) {
         if (k0 + KC + bq < it.lcount) {
           const int npid = pid_ahead;
-          cp_async_tpar(&s_tp[bq], w.tpar + npid);
+          cp_async_tpar(&s_tp[0][bq], KC * 16u, w.tpar + npid);
           s_pid[buf ^ 1][bq] = npid;
         } else {
-          s_tp[bq] = empty_tpar();
+          const TcPar z = empty_tpar();
+#pragma unroll
+          for (int k = 0; k < 4; ++k) s_tp[k][bq] = reinterpret_cast<const uint4*>(&z)[k];
           s_pid[buf ^ 1][bq] = 0;
         }
         cp_async_commit();
@@ -1390,7 +1410,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (has_next && bld) {
         cp_async_wait_all();
         const bool listed = k0 + KC + bq < it.lcount;
-        const TcPar& t = s_tp[bq];
+        TcPar t;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) reinterpret_cast<uint4*>(&t)[k] = s_tp[k][bq];
         const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][bq],
                                      s_spar[buf ^ 1][bq]);
         build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
@@ -1419,26 +1441,29 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         // the last drain left at zero, the cross terms (2^-8 .. 2^-16 of the
         // hi products) lose ulps of their own small sums; only the hi x hi
         // products, last, meet the full-size accumulator.
+        // the accumulator of K-step ks: the second working one for the
+        // upper half of a 64-particle three-piece stage
+        auto dk = [&](int ks) { return TWO_ACC && ks >= 2 ? d + (unsigned)TC_WB_COL : d; };
         if constexpr (NP == 3) {
           const unsigned long long a_3 = a_2 + (a_bytes >> 4);
           const unsigned long long b_3 = b_2 + (b_bytes >> 4);
 #pragma unroll
           for (int ks = 0; ks < KSTEPS; ++ks) {
             const unsigned ao = (unsigned)ks * 256u, bo = (unsigned)ks * bstep;
-            umma(d, a_2 + ao, b_2 + bo, id, 1u);   // mid mid
-            umma(d, a_hi + ao, b_3 + bo, id, 1u);  // hi lo
-            umma(d, a_3 + ao, b_hi + bo, id, 1u);  // lo hi
+            umma(dk(ks), a_2 + ao, b_2 + bo, id, 1u);   // mid mid
+            umma(dk(ks), a_hi + ao, b_3 + bo, id, 1u);  // hi lo
+            umma(dk(ks), a_3 + ao, b_hi + bo, id, 1u);  // lo hi
           }
         }
 #pragma unroll
         for (int ks = 0; ks < KSTEPS; ++ks) {
           const unsigned ao = (unsigned)ks * 256u, bo = (unsigned)ks * bstep;
-          umma(d, a_hi + ao, b_2 + bo, id, 1u);  // hi lo (pair) / hi mid
-          umma(d, a_2 + ao, b_hi + bo, id, 1u);  // lo hi (pair) / mid hi
+          umma(dk(ks), a_hi + ao, b_2 + bo, id, 1u);  // hi lo (pair) / hi mid
+          umma(dk(ks), a_2 + ao, b_hi + bo, id, 1u);  // lo hi (pair) / mid hi
         }
 #pragma unroll
         for (int ks = 0; ks < KSTEPS; ++ks)
-          umma(d, a_hi + (unsigned)ks * 256u, b_hi + (unsigned)ks * bstep, id, 1u);
+          umma(dk(ks), a_hi + (unsigned)ks * 256u, b_hi + (unsigned)ks * bstep, id, 1u);
         umma_commit(smem_u32(&bars[stage]));
       }
       pending_bits |= 1u << stage;
@@ -1498,6 +1523,16 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         } else {
           tmem_ld32(tmem + lane_base + (unsigned)c, r);
           tmem_wait_ld();
+          if (TWO_ACC) {
+            for (int h = 0; h < 32; h += 16) {
+              unsigned m[16];
+              tmem_ld16(tmem + lane_base + TC_WB_COL + (unsigned)(c + h), m);
+              tmem_wait_ld();
+#pragma unroll
+              for (int v = 0; v < 16; ++v)
+                r[h + v] = __float_as_uint(__uint_as_float(r[h + v]) + __uint_as_float(m[v]));
+            }
+          }
           if (drain) {
             for (int h = 0; h < 32; h += 16) {
               unsigned m[16];
@@ -1635,8 +1670,12 @@ int launch_contract_bf16x3(const Geo& g, const Ws& w, int num_sms, cudaStream_t 
   // stage size: the form's default unless the launch shape asks for 32
   const bool kc32 = g.kc == 32;
   int rc;
-  if (g.form == MG_FORM_BF16X6)
-    rc = launch_tc<SPLIT_BF16_3, 32>(g, w, num_sms, s, nwmax);
+  if (g.form == MG_FORM_BF16X6) {
+    // 64-particle stages hold two working accumulators of 128 columns
+    if (!kc32 && nwmax > TC_WB_COL) return MG_ERR_UNSUPPORTED;
+    rc = kc32 ? launch_tc<SPLIT_BF16_3, 32>(g, w, num_sms, s, nwmax)
+              : launch_tc<SPLIT_BF16_3, 64>(g, w, num_sms, s, nwmax);
+  }
   else if (g.form == MG_FORM_BF16X3)
     rc = kc32 ? launch_tc<SPLIT_BF16_2, 32>(g, w, num_sms, s, nwmax)
               : launch_tc<SPLIT_BF16_2, 64>(g, w, num_sms, s, nwmax);

@@ -22,7 +22,7 @@ def _problem(n=1000, nx=64, ny=64, nc=32, form=2, ngal=1):
 def test_candidates_per_form():
     from martini_gb300 import _native as N
     lib = N.load()
-    for form, count, kcs in ((N.MG_FORM_FP32, 4, {0}), (N.MG_FORM_BF16X6, 4, {0}),
+    for form, count, kcs in ((N.MG_FORM_FP32, 4, {0}), (N.MG_FORM_BF16X6, 8, {0, 32}),
                              (N.MG_FORM_F16X3, 8, {0, 32}), (N.MG_FORM_BF16X3, 8, {0, 32})):
         out = (N.Tuning * 16)()
         n = lib.mg_tuning_candidates(form, out, 16)
@@ -55,9 +55,11 @@ def test_cache_keys_store_lookup_reset():
                      (_problem(ngal=4), 200_000)):
         assert lib.mg_tuning_lookup(q, len(q), pairs, C.byref(got)) == 0
     # a shape the form cannot run is refused
-    bad = N.Tuning(64, 24, 1, 0)
+    bad = N.Tuning(48, 24, 1, 0)
     assert lib.mg_tuning_store(_problem(form=3), 1, 200_000, C.byref(bad)) == \
         N.MG_ERR_INVALID_ARGUMENT
+    assert lib.mg_tuning_store(_problem(form=0), 1, 200_000, C.byref(N.Tuning(32, 24, 1, 0))) \
+        == N.MG_ERR_INVALID_ARGUMENT
     assert lib.mg_tuning_store(p, 1, 200_000, C.byref(N.Tuning(0, 99, 1, 0))) == \
         N.MG_ERR_INVALID_ARGUMENT
     lib.mg_tuning_reset()
