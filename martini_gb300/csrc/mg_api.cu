@@ -67,7 +67,7 @@ struct Layout {
   size_t hdr, gal, gst, gp0, gt0, gs0, ge0, gr0, rec, tpar, npairs, pair_off, tile_count, tile_diff,
       tile_off, ehi, elo, inv_w, keys, list, keys_tmp, list_tmp, rs_hist,
       rs_off, scan_sums, seg_lo, seg_hi, seg_items, seg_part, item_off, part_off, partial,
-      flux_part, item_order, item_key, item_key_tmp, item_order_tmp, total;
+      flux_part, item_order, item_key, item_key_tmp, item_order_tmp, item_seg, total;
   long long cap_items;
 };
 
@@ -126,6 +126,7 @@ Layout layout(const Geo& g, long long cap_pairs, long long cap_partial) {
   L.item_key = take(sizeof(unsigned) * ci);
   L.item_key_tmp = take(sizeof(unsigned) * ci);
   L.item_order_tmp = take(sizeof(int) * ci);
+  L.item_seg = take(sizeof(int) * ci);
   L.partial = take(sizeof(float) * (size_t)TILE_PX * g.max_width *
                    (size_t)(cap_partial > 0 ? cap_partial : 0));
   L.total = o;
@@ -174,6 +175,7 @@ Ws make_ws(void* base, const Layout& L) {
   w.item_key = reinterpret_cast<unsigned*>(b + L.item_key);
   w.item_key_tmp = reinterpret_cast<unsigned*>(b + L.item_key_tmp);
   w.item_order_tmp = reinterpret_cast<int*>(b + L.item_order_tmp);
+  w.item_seg = reinterpret_cast<int*>(b + L.item_seg);
   w.cap_items = L.cap_items;
   return w;
 }

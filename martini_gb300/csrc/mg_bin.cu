@@ -527,6 +527,7 @@ __global__ void k_item_keys(Geo g, Ws w) {
       // all keys equal: the stable sort keeps segment order
       w.item_key[base + k] = g.cost_order ? 65535u - (unsigned)q : 0u;
       w.item_order[base + k] = (int)(base + k);
+      w.item_seg[base + k] = sg;
     }
   }
 }

@@ -13,17 +13,6 @@ constexpr int F32_THREADS = 256;
 constexpr int F32_KC = 32;  // particles per shared-memory chunk
 constexpr int F32_MASTER_BYTES = 32 * F32_THREADS * 4;  // master accumulators (dynamic)
 
-// Segment of work item `item`: the largest sg with item_off[sg] <= item
-// (segments without items share their successor's offset).
-__device__ __forceinline__ int find_segment(const long long* item_off, int nseg, long long item) {
-  int a = 0, b = nseg;
-  while (b - a > 1) {
-    int m = (a + b) >> 1;
-    if (item_off[m] <= item) a = m; else b = m;
-  }
-  return a;
-}
-
 struct ItemInfo {
   int seg, gal, tile, tx, ty, kc, nk;  // tile: within the cube
   int c0;            // first channel of this item's block
@@ -34,7 +23,7 @@ struct ItemInfo {
 __device__ __forceinline__ ItemInfo decode_item(const Geo& g, const Ws& w, long long item,
                                                 int kch) {
   ItemInfo it;
-  const int sg = find_segment(w.item_off, g.nseg, item);
+  const int sg = w.item_seg[item];
   it.seg = sg;
   it.gal = find_gal(w.gs0, g.ngal, sg);
   const Gal& G = w.gal[it.gal];

@@ -246,6 +246,7 @@ struct Ws {
   unsigned* item_key;    // [cap_items]
   unsigned* item_key_tmp;
   int* item_order_tmp;
+  int* item_seg;         // [cap_items] segment of each item (in item index order)
   long long cap_items;
 };
 

@@ -287,11 +287,7 @@ struct ItemTC {
 };
 
 __device__ __forceinline__ ItemTC decode_tc(const Geo& g, const Ws& w, long long item, int kch) {
-  int a = 0, b = g.nseg;
-  while (b - a > 1) {
-    int m = (a + b) >> 1;
-    if (w.item_off[m] <= item) a = m; else b = m;
-  }
+  const int a = w.item_seg[item];
   ItemTC it;
   it.seg = a;
   it.gal = find_gal(w.gs0, g.ngal, a);
@@ -1055,6 +1051,20 @@ __device__ __forceinline__ void s_task_store(const unsigned (&v)[8], int g8, int
   }
 }
 
+// Prefetch into L2 the part of a listed particle's spectrum-store row that
+// falls in the block [cb0, cb1] (one prefetch per 128-byte line): the
+// spectrum tasks of its stage read it a stage later.
+__device__ __forceinline__ void prefetch_row(const unsigned* spec, const TcPar& t, bool listed,
+                                             int cb0, int cb1) {
+  if (spec == nullptr || !listed || t.kind == 0) return;
+  const int a = max(t.clo, cb0), b = min(t.chi, cb1);
+  if (a > b) return;
+  const char* p = reinterpret_cast<const char*>(spec + t.soff + (a - t.clo));
+  const char* e = reinterpret_cast<const char*>(spec + t.soff + (b - t.clo));
+  for (; p < e; p += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(e));
+}
+
 // What a build warp tells the others about its 32 particles of a stage:
 // the union of their supports and the path of each of its 8-particle groups.
 // Lane l holds particle l (kind 0 for an empty slot).
@@ -1236,12 +1246,16 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   unsigned phase_bits = 0u, pending_bits = 0u;
   int stage = 0;
   int since_drain = 0;
+  // thread 0 takes the next item from the queue while this one runs (the
+  // atomic's round trip is off the item switch)
+  long long next_item = tid == 0 ? (long long)atomicAdd(&w.hdr->item_counter, 1u) : 0;
 
   for (;;) {
-    if (tid == 0) s_item = (long long)atomicAdd(&w.hdr->item_counter, 1u);
+    if (tid == 0) s_item = next_item;
     __syncthreads();
     const long long item = s_item;
     if (item >= n_items || s_abort) break;
+    if (tid == 0) next_item = (long long)atomicAdd(&w.hdr->item_counter, 1u);
     // the queue runs over the items in cost order, largest first
     const ItemTC it = decode_tc(g, w, (long long)w.item_order[item], kch);
     const Gal& G = w.gal[it.gal];
@@ -1283,6 +1297,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       }
       if (KC + bq < it.lcount) pid_ahead = w.list[it.lbeg + KC + bq];
       const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[0][bq], s_spar[0][bq]);
+      prefetch_row(spec, t, listed, cb0, cb1);
       build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
                     &s_win[0][bq >> 5], &s_gp[0][(bq >> 5) * 4]);
     }
@@ -1415,6 +1430,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         for (int k = 0; k < 4; ++k) reinterpret_cast<uint4*>(&t)[k] = s_tp[k][bq];
         const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][bq],
                                      s_spar[buf ^ 1][bq]);
+        prefetch_row(spec, t, listed, cb0, cb1);
         build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
                       &s_win[buf ^ 1][bq >> 5], &s_gp[buf ^ 1][(bq >> 5) * 4]);
       }
