@@ -104,6 +104,13 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar)
+      : "memory");
+}
+
 // Bounded wait; returns false on timeout.
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
   for (unsigned i = 0; i < TC_SPIN_LIMIT; ++i)
@@ -1127,6 +1134,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
   __shared__ float4 s_gtab[GT_NCELL + 1];  // Gaussian truncation cells
   __shared__ __align__(8) unsigned long long bars[2];
+  // s_full[b]: every warp has produced its part of the stage in buffer b
+  // (the MMA warp then issues it); s_parb[b]: the build warps have written
+  // the parameters of the stage in buffer b
+  __shared__ __align__(8) unsigned long long s_full[2], s_parb[2];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
   __shared__ int s_abort;
@@ -1172,6 +1183,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   if (tid == 0) {
     mbar_init(smem_u32(&bars[0]), 1);
     mbar_init(smem_u32(&bars[1]), 1);
+    mbar_init(smem_u32(&s_full[0]), NWARP);
+    mbar_init(smem_u32(&s_full[1]), NWARP);
+    mbar_init(smem_u32(&s_parb[0]), NB);
+    mbar_init(smem_u32(&s_parb[1]), NB);
     s_abort = 0;
   }
   if (warp == 0) {
@@ -1208,9 +1223,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   // written since the last drain; no MMA in flight
   // The drain of columns [lo, hi): the warps of a lane quarter take its
   // 16-column pieces round robin (a column past what the MMAs wrote is zero
-  // and adds nothing).  A build warp (column group 3 of the last NB
-  // quarters) leaves its quarter's pieces to the other three.
-  const int dwarps = quarter >= 4 - NB ? 3 : 4;
+  // and adds nothing).  The MMA and build warps (column group 3 of the last
+  // quarters) leave their quarters' pieces to the other three.
+  const int dwarps = quarter >= MMA_WARP - 12 ? 3 : 4;
   auto drain_tmem = [&](int lo, int hi) {
     if (colgrp >= dwarps) return;
     for (int c = (lo & ~15) + 16 * colgrp; c < hi; c += 16 * dwarps) {
@@ -1244,6 +1259,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   // of pending_bits says MMAs reading it are in flight (registers, not a
   // dynamically indexed array)
   unsigned phase_bits = 0u, pending_bits = 0u;
+  // bit b: parity of the next phase of s_full[b] / s_parb[b] to complete
+  unsigned full_par = 0u, parb_par = 0u;
   int stage = 0;
   int since_drain = 0;
   // thread 0 takes the next item from the queue while this one runs (the
@@ -1313,20 +1330,25 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         phase_bits ^= 1u << stage;
         pending_bits &= ~(1u << stage);
       }
+      // the stage's parameters: built at the item's start for its first
+      // stage, else by the build warps during the previous stage
+      if (ch > 0) {
+        if (!mbar_wait(smem_u32(&s_parb[buf]), (parb_par >> buf) & 1u)) s_abort = 1;
+        parb_par ^= 1u << buf;
+      }
       // the next stage's records travel global -> shared by cp.async while
       // this one is produced (its list entry was read a stage earlier); the
       // list entry of the stage after is read now
       const bool has_next = ch + 1 < nchunk;
+      int npid = 0;
       if (has_next && bld) {
         if (k0 + KC + bq < it.lcount) {
-          const int npid = pid_ahead;
+          npid = pid_ahead;
           cp_async_tpar(&s_tp[0][bq], KC * 16u, w.tpar + npid);
-          s_pid[buf ^ 1][bq] = npid;
         } else {
           const TcPar z = empty_tpar();
 #pragma unroll
           for (int k = 0; k < 4; ++k) s_tp[k][bq] = reinterpret_cast<const uint4*>(&z)[k];
-          s_pid[buf ^ 1][bq] = 0;
         }
         cp_async_commit();
         if (k0 + 2 * KC + bq < it.lcount) pid_ahead = w.list[it.lbeg + k0 + 2 * KC + bq];
@@ -1374,14 +1396,13 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       constexpr int PXL = KC / 32;  // pixels per lane
       constexpr int NG8 = KC / 8;   // particle groups of a stage
       const int wa = it.c0 + w0;    // first window channel (absolute)
-      // Spectrum tasks: the first NSW go to warps 0 .. NSW - 1, the next
-      // NSW + 1 back from the MMA warp (NSW) to warp 0, so that a second task
-      // lands on the warps with the least other work first; the rest round
-      // robin over warps 0 .. NSW.  The loads of a warp's first task are in
-      // flight during its weights.
+      // Spectrum tasks go to warps 0 .. NSW - 1 in rounds of NSW, every
+      // other round in reverse order, so that the warps' counts differ by
+      // one at most and the extra tasks do not pile up on the same warps.
+      // The loads of a warp's first task are in flight during its weights.
       const int n_chunks = (nw + 31) >> 5;
       const int n_stasks = spec ? n_chunks * NG8 : 0;
-      const int t0 = warp < NSW ? warp : (warp == NSW ? NSW : n_stasks);
+      const int t0 = warp < NSW ? warp : n_stasks;
       unsigned sv[8];
       if (t0 < n_stasks)
         s_task_load(s_spar[buf] + 8 * (t0 % NG8), spec, wa, 32 * (t0 / NG8) + lane, sv);
@@ -1397,8 +1418,8 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       if (spec) {
         // Gaussian lines from the spectrum store: tasks of (32-channel
         // chunk, 8-particle group), round robin over the warps
-        for (int t = t0; t < n_stasks;
-             t = t < NSW ? 2 * NSW - t : (t <= 2 * NSW ? 2 * NSW + 1 + warp : t + NSW + 1)) {
+        for (int t = t0, r = 0; t < n_stasks;
+             ++r, t = r * NSW + ((r & 1) ? NSW - 1 - warp : warp)) {
           const int g8 = t % NG8, n = 32 * (t / NG8) + lane;
           if (t != t0) s_task_load(s_spar[buf] + 8 * g8, spec, wa, n, sv);
           if (n < nw) s_task_store<SPLIT>(sv, g8, n, nw, sb, b_bytes);
@@ -1423,6 +1444,12 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         }
       }
       if (has_next && bld) {
+        // the next stage's buffer of parameters was last read in the
+        // previous stage: every warp must have finished it
+        if (ch > 0 && !mbar_wait(smem_u32(&s_full[stage ^ 1]),
+                                 ((full_par >> (stage ^ 1)) & 1u) ^ 1u))
+          s_abort = 1;
+        s_pid[buf ^ 1][bq] = npid;
         cp_async_wait_all();
         const bool listed = k0 + KC + bq < it.lcount;
         TcPar t;
@@ -1433,11 +1460,19 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         prefetch_row(spec, t, listed, cb0, cb1);
         build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
                       &s_win[buf ^ 1][bq >> 5], &s_gp[buf ^ 1][(bq >> 5) * 4]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&s_parb[buf ^ 1]));
       }
+      // hand the stage over: operands to the async proxy, drains before the
+      // next MMAs, then one arrival per warp; no warp waits for the others
       fence_proxy_async();
-      __syncthreads();
-      if (s_abort) break;
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&s_full[stage]));
+      const unsigned fpar = (full_par >> stage) & 1u;
+      full_par ^= 1u << stage;
       if (tid == MMA_WARP * 32) {
+        if (!mbar_wait(smem_u32(&s_full[stage]), fpar)) s_abort = 1;
         tc_fence_after();
         // nw <= nwmax <= 256: one MMA spans the window.  The descriptors'
         // start-address field (bits 0-13, address / 16) steps by adding the
@@ -1482,6 +1517,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
           umma(dk(ks), a_hi + (unsigned)ks * 256u, b_hi + (unsigned)ks * bstep, id, 1u);
         umma_commit(smem_u32(&bars[stage]));
       }
+      if (s_abort) break;
       pending_bits |= 1u << stage;
       stage ^= 1;
       if (drain && ++since_drain == DRAIN_STAGES && ch + 1 < nchunk) {
