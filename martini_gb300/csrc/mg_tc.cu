@@ -1382,7 +1382,11 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       unsigned char* const sb = sa + NP * a_bytes;
       // drain of the previous interval: the MMAs of the previous stage are
       // waited for, then the working accumulator is added into the master
+      // (a warp with no pieces to drain does not wait: the stage's buffer
+      // stays pending until the warp next needs it)
       auto drain_now = [&]() {
+        drain_due = false;
+        if (colgrp >= dwarps) return;
         const int sp = stage ^ 1;  // the previous stage's buffer
         if (!mbar_wait(smem_u32(&bars[sp]), (phase_bits >> sp) & 1u)) s_abort = 1;
         phase_bits ^= 1u << sp;
@@ -1390,7 +1394,6 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         tc_fence_after();
         drain_tmem(p_lo, p_hi);
         tc_fence_before();
-        drain_due = false;
       };
       // ---- A = W: one 8-particle group x pixel group per warp
       constexpr int PXL = KC / 32;  // pixels per lane
@@ -1412,8 +1415,6 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       produce_w_task<SPLIT, PXL>(s_par[buf] + 8 * (warp % NG8), path, s_ks,
                                  smem_u32(s_ktab), gtab_s32, ucap, warp % NG8, warp / NG8, lane, sa,
                                  a_bytes);
-      // the drain of the previous interval: its MMAs are done by now
-      if (drain_due) drain_now();  // block-uniform
       // ---- B = S
       if (spec) {
         // Gaussian lines from the spectrum store: tasks of (32-channel
@@ -1463,6 +1464,9 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&s_parb[buf ^ 1]));
       }
+      // the drain of the previous interval, last: its MMAs have had the
+      // whole production of this stage to complete
+      if (drain_due) drain_now();
       // hand the stage over: operands to the async proxy, drains before the
       // next MMAs, then one arrival per warp; no warp waits for the others
       fence_proxy_async();
