@@ -1125,11 +1125,14 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   // piece k of slot q at s_tp[k][q], so that a warp's 16-byte reads of one
   // piece are contiguous
   __shared__ __align__(16) uint4 s_tp[4][KC];
-  __shared__ int s_pid[2][KC];
-  __shared__ int2 s_win[2][NB];    // support union [clo, chi] per build warp (window)
-  __shared__ int s_gp[2][KC / 8];  // path of each 8-particle group (GP_*)
-  __shared__ __align__(16) StagePar s_par[2][KC];  // weight producers' view of a stage
-  __shared__ __align__(16) SPar s_spar[2][KC];     // spectrum producers' view
+  // Stage parameters rotate over three buffers (stage ch in buffer ch % 3
+  // of its item): the build warps write a stage's while the warps still
+  // finishing the stage before the previous one read theirs.
+  __shared__ int s_pid[3][KC];
+  __shared__ int2 s_win[3][NB];    // support union [clo, chi] per build warp (window)
+  __shared__ int s_gp[3][KC / 8];  // path of each 8-particle group (GP_*)
+  __shared__ __align__(16) StagePar s_par[3][KC];  // weight producers' view of a stage
+  __shared__ __align__(16) SPar s_spar[3][KC];     // spectrum producers' view
   __shared__ KSpec s_ks[MG_MAX_KERNELS];
   __shared__ float4 s_ktab[KT_SMEM_CELLS];
   __shared__ float4 s_gtab[GT_NCELL + 1];  // Gaussian truncation cells
@@ -1137,7 +1140,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
   // s_full[b]: every warp has produced its part of the stage in buffer b
   // (the MMA warp then issues it); s_parb[b]: the build warps have written
   // the parameters of the stage in buffer b
-  __shared__ __align__(8) unsigned long long s_full[2], s_parb[2];
+  __shared__ __align__(8) unsigned long long s_full[2], s_parb[3];
   __shared__ unsigned s_tmem;
   __shared__ long long s_item;
   __shared__ int s_abort;
@@ -1187,6 +1190,7 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     mbar_init(smem_u32(&s_full[1]), NWARP);
     mbar_init(smem_u32(&s_parb[0]), NB);
     mbar_init(smem_u32(&s_parb[1]), NB);
+    mbar_init(smem_u32(&s_parb[2]), NB);
     s_abort = 0;
   }
   if (warp == 0) {
@@ -1317,11 +1321,13 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
       prefetch_row(spec, t, listed, cb0, cb1);
       build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
                     &s_win[0][bq >> 5], &s_gp[0][(bq >> 5) * 4]);
+      if (KC + bq < it.lcount) asm volatile("prefetch.global.L2 [%0];" ::"l"(w.tpar + pid_ahead));
     }
     __syncthreads();
 
     for (int ch = 0; ch < nchunk; ++ch) {
-      const int buf = ch & 1;
+      const int buf = ch % 3;              // this stage's parameters
+      const int nbuf = buf == 2 ? 0 : buf + 1;  // the next stage's
       const int k0 = ch * KC;
       const int kn = min(KC, it.lcount - k0);
       // the stage must be free: every thread waits for the MMAs that last read it
@@ -1445,24 +1451,29 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
         }
       }
       if (has_next && bld) {
-        // the next stage's buffer of parameters was last read in the
-        // previous stage: every warp must have finished it
-        if (ch > 0 && !mbar_wait(smem_u32(&s_full[stage ^ 1]),
-                                 ((full_par >> (stage ^ 1)) & 1u) ^ 1u))
+        // the next stage's buffer of parameters was last read two stages
+        // ago: every warp must have finished that stage (s_full[stage]'s
+        // phase before the current one)
+        if (ch > 1 &&
+            !mbar_wait(smem_u32(&s_full[stage]), ((full_par >> stage) & 1u) ^ 1u))
           s_abort = 1;
-        s_pid[buf ^ 1][bq] = npid;
+        s_pid[nbuf][bq] = npid;
         cp_async_wait_all();
         const bool listed = k0 + KC + bq < it.lcount;
         TcPar t;
 #pragma unroll
         for (int k = 0; k < 4; ++k) reinterpret_cast<uint4*>(&t)[k] = s_tp[k][bq];
-        const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[buf ^ 1][bq],
-                                     s_spar[buf ^ 1][bq]);
+        const int kind = build_stage(t, listed, i0, j0, cb0, cb1, s_par[nbuf][bq],
+                                     s_spar[nbuf][bq]);
         prefetch_row(spec, t, listed, cb0, cb1);
         build_summary(listed ? t.clo : 0x7fffffff, listed ? t.chi : -1, kind, lane,
-                      &s_win[buf ^ 1][bq >> 5], &s_gp[buf ^ 1][(bq >> 5) * 4]);
+                      &s_win[nbuf][bq >> 5], &s_gp[nbuf][(bq >> 5) * 4]);
+        // the particle of the stage after next into L2: its cp.async, at the
+        // next stage's start, then misses HBM no more
+        if (k0 + 2 * KC + bq < it.lcount)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(w.tpar + pid_ahead));
         __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&s_parb[buf ^ 1]));
+        if (lane == 0) mbar_arrive(smem_u32(&s_parb[nbuf]));
       }
       // the drain of the previous interval, last: its MMAs have had the
       // whole production of this stage to complete
