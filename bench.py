@@ -49,9 +49,9 @@ L2_BYTES = 129 * 1024 * 1024
 # contraction forms (the MG_FORM_* codes)
 FORMS = {"fp32": 0, "bf16x3": 1, "f16x3": 2, "bf16x6": 3}
 # DRAM bytes (read + write) of one launch of the contraction kernel, from
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the full workload;
-# profiles/k_contract_tc_disc1m_512_f16x3.md gives the command and figures
-TRAFFIC_BYTES = {("disc1m_512", "f16x3"): 2_895_373_312}
+# one ncu pass (dram__bytes_read.sum + dram__bytes_write.sum) on the full
+# workload, for the kernel as it stands
+TRAFFIC_BYTES = {("disc4m_1024", "bf16x6"): 5_896_006_400}
 
 
 def launches_per_step(form: str, gaussian: bool, nx: int, ny: int, nc: int, ngal: int = 1,
