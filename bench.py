@@ -732,91 +732,97 @@ def run_population(a, rank, world, local, dev):
     t_loop32 = timed(looped_fp32, max(1, min(a.steps, 3)))
     batch.run_stages(N.MG_STAGE_BIN | N.MG_STAGE_SPEC)
     t_contract = float(np.mean(timed(lambda: batch.run_stages(N.MG_STAGE_CONTRACT), 3)))
-    # end to end: particles from pinned host memory, every cube back.  Two
-    # buffer sets (device particles and cubes, each with its batched problem;
-    # pinned host cubes) so that the copies of one batch overlap the
-    # insertion of the other: uploads and read-backs run on their own
-    # streams, insertions in order on the compute stream
-    import dataclasses
-    host = []
-    for it in items:
-        w = it["w"]
-        hp = {k: torch.from_numpy(np.ascontiguousarray(w[k], dtype=dt)).pin_memory()
-              for k, dt in (("x", np.float64), ("y", np.float64), ("sm_range", np.float64),
-                            ("h_eff", np.float32), ("v", np.float64), ("amp", np.float64))}
-        if w["kernel_index"] is not None:
-            hp["kernel_index"] = torch.from_numpy(w["kernel_index"].astype(np.int8)).pin_memory()
-        if w["sigma"] is not None:
-            hp["sigma"] = torch.from_numpy(w["sigma"].astype(np.float32)).pin_memory()
-        host.append(hp)
-    h2d = sum(t.numel() * t.element_size() for hp in host for t in hp.values())
-    d2h = sum(it["cube"].numel() * 4 for it in items)
-    sets = [dict(batch=batch, dev=[{k: getattr(it["parts"], k) for k in hp}
-                                   for it, hp in zip(items, host)],
-                 cubes=[it["cube"] for it in items])]
-    items1, probs1 = [], []
-    for it, hp in zip(items, host):
-        w = it["w"]
-        # the second set starts as a copy of the first (the plan sizes its
-        # workspace from the particles it bins)
-        p1 = dataclasses.replace(it["parts"], **{k: getattr(it["parts"], k).clone()
-                                                for k in hp})
-        cube1, flux1 = torch.empty_like(it["cube"]), torch.empty_like(it["flux"])
-        probs1.append(eng.problem(p1, w["kernels"], w["spectral_model"], w["sigma_const"],
-                                  w["nx"], w["ny"], w["nc"], 0, 0, it["edges"], cube1, flux1,
-                                  form))
-        items1.append(dict(parts=p1, cube=cube1, flux=flux1))
-    batch1 = BatchInsertion(eng, probs1, keep=items1)
-    batch1.plan()
-    sets.append(dict(batch=batch1, dev=[{k: getattr(it1["parts"], k) for k in hp}
-                                        for it1, hp in zip(items1, host)],
-                     cubes=[it1["cube"] for it1 in items1]))
-    for st in sets:
-        st["host_cubes"] = [torch.empty(tuple(c.shape), dtype=torch.float32).pin_memory()
-                            for c in st["cubes"]]
-    up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    comp_ev, down_ev = {}, {}
+    def pop_e2e():
+        # end to end: particles from pinned host memory, every cube back.  Two
+        # buffer sets (device particles and cubes, each with its batched problem;
+        # pinned host cubes) so that the copies of one batch overlap the
+        # insertion of the other: uploads and read-backs run on their own
+        # streams, insertions in order on the compute stream
+        import dataclasses
+        host = []
+        for it in items:
+            w = it["w"]
+            hp = {k: torch.from_numpy(np.ascontiguousarray(w[k], dtype=dt)).pin_memory()
+                  for k, dt in (("x", np.float64), ("y", np.float64), ("sm_range", np.float64),
+                                ("h_eff", np.float32), ("v", np.float64), ("amp", np.float64))}
+            if w["kernel_index"] is not None:
+                hp["kernel_index"] = torch.from_numpy(w["kernel_index"].astype(np.int8)).pin_memory()
+            if w["sigma"] is not None:
+                hp["sigma"] = torch.from_numpy(w["sigma"].astype(np.float32)).pin_memory()
+            host.append(hp)
+        h2d = sum(t.numel() * t.element_size() for hp in host for t in hp.values())
+        d2h = sum(it["cube"].numel() * 4 for it in items)
+        sets = [dict(batch=batch, dev=[{k: getattr(it["parts"], k) for k in hp}
+                                       for it, hp in zip(items, host)],
+                     cubes=[it["cube"] for it in items])]
+        items1, probs1 = [], []
+        for it, hp in zip(items, host):
+            w = it["w"]
+            # the second set starts as a copy of the first (the plan sizes its
+            # workspace from the particles it bins)
+            p1 = dataclasses.replace(it["parts"], **{k: getattr(it["parts"], k).clone()
+                                                    for k in hp})
+            cube1, flux1 = torch.empty_like(it["cube"]), torch.empty_like(it["flux"])
+            probs1.append(eng.problem(p1, w["kernels"], w["spectral_model"], w["sigma_const"],
+                                      w["nx"], w["ny"], w["nc"], 0, 0, it["edges"], cube1, flux1,
+                                      form))
+            items1.append(dict(parts=p1, cube=cube1, flux=flux1))
+        batch1 = BatchInsertion(eng, probs1, keep=items1)
+        batch1.plan()
+        sets.append(dict(batch=batch1, dev=[{k: getattr(it1["parts"], k) for k in hp}
+                                            for it1, hp in zip(items1, host)],
+                         cubes=[it1["cube"] for it1 in items1]))
+        for st in sets:
+            st["host_cubes"] = [torch.empty(tuple(c.shape), dtype=torch.float32).pin_memory()
+                                for c in st["cubes"]]
+        up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+        comp_ev, down_ev = {}, {}
 
-    def e2e_step(k):
-        st = sets[k % 2]
-        # inputs of batch k: after the insertion that last read this set
-        if k - 2 in comp_ev:
-            up.wait_event(comp_ev[k - 2])
-        with torch.cuda.stream(up):
-            for hp, dp in zip(host, st["dev"]):
-                for key, t in hp.items():
-                    dp[key].copy_(t, non_blocking=True)
-        stream.wait_event(up.record_event())
-        # the insertion overwrites this set's cubes: after their read-back
-        if k - 2 in down_ev:
-            stream.wait_event(down_ev[k - 2])
-        st["batch"].run(stream=stream)
-        comp_ev[k] = stream.record_event()
-        down.wait_event(comp_ev[k])
-        with torch.cuda.stream(down):
-            for hc, c in zip(st["host_cubes"], st["cubes"]):
-                hc.copy_(c, non_blocking=True)
-        down_ev[k] = down.record_event()
+        def e2e_step(k):
+            st = sets[k % 2]
+            # inputs of batch k: after the insertion that last read this set
+            if k - 2 in comp_ev:
+                up.wait_event(comp_ev[k - 2])
+            with torch.cuda.stream(up):
+                for hp, dp in zip(host, st["dev"]):
+                    for key, t in hp.items():
+                        dp[key].copy_(t, non_blocking=True)
+            stream.wait_event(up.record_event())
+            # the insertion overwrites this set's cubes: after their read-back
+            if k - 2 in down_ev:
+                stream.wait_event(down_ev[k - 2])
+            st["batch"].run(stream=stream)
+            comp_ev[k] = stream.record_event()
+            down.wait_event(comp_ev[k])
+            with torch.cuda.stream(down):
+                for hc, c in zip(st["host_cubes"], st["cubes"]):
+                    hc.copy_(c, non_blocking=True)
+            down_ev[k] = down.record_event()
 
-    e2e_step(0)
-    e2e_step(1)
-    torch.cuda.synchronize()
-    comp_ev.clear()
-    down_ev.clear()
-    ke = max(2, min(a.steps, 4))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    up.wait_event(e0)
-    down.wait_event(e0)
-    for k in range(ke):
-        e2e_step(k)
-    stream.wait_event(down_ev[ke - 1])
-    stream.wait_event(down_ev[ke - 2])
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t_e2e = e0.elapsed_time(e1) / 1e3 / ke
-    batch1.check()
+        e2e_step(0)
+        e2e_step(1)
+        torch.cuda.synchronize()
+        comp_ev.clear()
+        down_ev.clear()
+        ke = max(2, min(a.steps, 4))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        up.wait_event(e0)
+        down.wait_event(e0)
+        for k in range(ke):
+            e2e_step(k)
+        stream.wait_event(down_ev[ke - 1])
+        stream.wait_event(down_ev[ke - 2])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_e2e = e0.elapsed_time(e1) / 1e3 / ke
+        batch1.check()
+        return t_e2e, h2d, d2h
+
+    # (skipped with --no-e2e: it holds a second set of particles, cubes and
+    # workspace, which the full 2000-galaxy population cannot spare)
+    t_e2e, h2d, d2h = (float("nan"), 0, 0) if a.no_e2e else pop_e2e()
     tb, tl = float(np.sum(t_batch)), float(np.sum(t_loop))
     if world > 1:
         tt = torch.tensor([tb, tl, t_e2e], dtype=torch.float64, device=dev)
