@@ -1,28 +1,35 @@
 // Split-precision tensor-core contraction (tcgen05, sm_103a).
 //
 // One persistent CTA (16 warps) per SM walks the work items (tile, K chunk).
-// For each stage of KC particles of the tile's (tile, clo)-sorted list the
-// 512 threads build in shared memory
+// For each stage of KC particles of the tile's list (sorted by kernel class,
+// then first channel) the warps build in shared memory
 //   A = W[128 pixels][KC particles]        (kernel pixel integrals)
 //   B = S[Nw channels][KC particles]       (spectra over the stage's window)
 // each split into 16-bit pieces: a hi + lo pair (bf16, or fp16 after exact
 // power-of-two scaling), or the exact three-piece BF16 split hi + mid + lo of
 // the FP32 value.  The pieces are stored K-major in the no-swizzle canonical
 // layout (8-row x 16-byte core matrices; K-direction stride 128 B, row-group
-// stride 256 B).  Thread 0 issues the products per 16-particle step -- three
-// for a pair (W_hi S_hi + W_hi S_lo + W_lo S_hi), six for three pieces (every
-// cross term down to 2^-16 relative: hh, hm, mh, mm, hl, lh) -- as
-// tcgen05.mma (kind::f16, FP32 accumulate) into a TMEM accumulator holding
-// the tile's whole band (128 lanes = pixels, columns = channels), at the
-// stage's column window.  Two shared-memory stages alternate: producers fill
-// one while the tensor core reads the other, and tcgen05.commit arrives on the
-// stage's mbarrier when it may be reused.  The records of the next stage
-// travel global -> shared by cp.async while the current one is produced.
-// Every two stages the working accumulator is drained (round to nearest) into
-// a master accumulator in the other half of TMEM, halfway through the next
-// stage's production.  The epilogue reads TMEM with tcgen05.ld and writes
-// 128-byte channel runs of each pixel to the cube, or to a split-K partial
-// buffer.
+// stride 256 B).  One thread of the MMA warp issues the products per
+// 16-particle step -- three for a pair (W_hi S_hi + W_hi S_lo + W_lo S_hi),
+// six for three pieces (every cross term down to 2^-16 relative: hh, hm, mh,
+// mm, hl, lh) -- as tcgen05.mma (kind::f16, FP32 accumulate) into a TMEM
+// accumulator holding the tile's block (128 lanes = pixels, columns =
+// channels), at the stage's column window.
+//
+// Roles: every warp computes one weight task per stage; the build warps also
+// copy the next stage's particle parameters (cp.async) and turn them into
+// stage parameters; the other warps take the spectrum tasks and the drains.
+// Stages are handed over by mbarriers, not block barriers: each warp arrives
+// on the stage's mbarrier when its part is written, the MMA thread waits for
+// all of them, and tcgen05.commit arrives on the stage buffer's mbarrier when
+// the buffer may be written again.  Two shared-memory stage buffers
+// alternate; stage parameters rotate over three.
+//
+// Every stage (three pieces) or every two (pairs) the working accumulator is
+// drained (round to nearest) into a master accumulator in the other half of
+// TMEM, as the last step of the next stage.  The epilogue reads TMEM with
+// tcgen05.ld and writes 128-byte channel runs of each pixel to the cube, or
+// to a split-K partial buffer.
 //
 // Every mbarrier wait has an iteration limit: on expiry the kernel sets
 // ST_TIMEOUT, frees its TMEM and returns.
@@ -1296,9 +1303,10 @@ k_contract_tc(Geo g, Ws w, int nwmax) {
     const int i0 = it.tx * TILE_I, j0 = it.ty * TILE_J;
     const int nchunk = (it.lcount + KC - 1) / KC;
     int d_lo = 0x7fffffff, d_hi = 0;  // columns written since the last drain
-    // a drain scheduled after a stage's MMAs runs halfway through the next
-    // stage's production, when those MMAs have completed (no MMA of the next
-    // stage is issued before its barrier), over columns [p_lo, p_hi)
+    // a drain scheduled after a stage's MMAs runs as the last step of the
+    // next stage's production, once those MMAs have completed (the next
+    // stage's MMAs wait for every warp's arrival, drains included), over
+    // columns [p_lo, p_hi)
     bool drain_due = false;
     int p_lo = 0, p_hi = 0;
     int t_lo = 0x7fffffff, t_hi = 0;  // columns written by this item
