@@ -114,3 +114,54 @@ def test_tuned_insertion_matches_oracle(form):
     assert np.abs(out - ref).max() / np.abs(ref).max() <= 1e-5
     assert abs(flux[0].item() - ref.sum()) / ref.sum() <= 1e-6
     lib.mg_tuning_reset()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [2, 3], ids=["f16x3", "bf16x6"])
+def test_every_candidate_shape_matches_oracle(form):
+    """Each candidate launch shape of the form -- 64- and 32-particle stages
+    (for bf16x6: two working accumulators, or one), 24 or 12 items per SM,
+    cost-ordered or segment-ordered queue -- stored for the problem's class
+    and used by the insertion, stays within 1e-5 of peak and 1e-6 of flux."""
+    from martini_gb300 import _native as N
+    from martini_gb300.engine import DeviceParticles, InsertionEngine
+    import torch
+    lib = N.load()
+    lib.mg_tuning_reset()
+    rng = np.random.default_rng(22)
+    n, nx, ny, nc = 15000, 48, 64, 160  # two channel blocks for bf16x6
+    kernels = orc.adaptive_tuple("WendlandC2Kernel")
+    h = 10 ** rng.uniform(-0.3, 0.9, n)
+    kidx, size, resc = orc.select_kernels(kernels, h)
+    x, y = rng.normal(24, 7, n), rng.normal(32, 9, n)
+    ranges = orc.sm_ranges(h, size)
+    v, sig = rng.normal(0, 120, n), rng.uniform(4, 12, n)
+    mhi = 10 ** rng.uniform(4, 5, n)
+    amp = mhi / 9.0 / orc.MHI_TO_JY
+    edges = orc.vrad_channel_edges(nc, 4.0, 0.0)
+    spectra = orc.init_spectra("gaussian", mhi, np.full(n, 3.0), v, edges, sig)
+    ref = orc.insert_scatter(nx, ny, x, y, ranges, kernels, kidx, h * resc, spectra)
+    eng = InsertionEngine("cuda:0")
+    parts = DeviceParticles.from_host(eng.device, x, y, ranges, h * resc, kidx, v=v, sigma=sig,
+                                      amp=amp)
+    e = torch.from_numpy(edges).to(eng.device)
+    table = [(N.MG_KERNEL_WENDLAND_C2, 0.0), (N.MG_KERNEL_DIRAC, 0.0), (N.MG_KERNEL_GAUSSIAN, 6.0)]
+    cube = torch.empty((nx, ny, nc), dtype=torch.float32, device=eng.device)
+    flux = torch.empty(nc + 1, dtype=torch.float64, device=eng.device)
+    prob = eng.problem(parts, table, N.MG_SPECTRUM_GAUSSIAN, 0.0, nx, ny, nc, 0, 0, e, cube, flux,
+                       form)
+    info = eng.plan(prob)
+    cands = (N.Tuning * 16)()
+    k = lib.mg_tuning_candidates(form, cands, 16)
+    assert {t.kc for t in cands[:k]} == {0, 32}
+    for t in cands[:k]:
+        assert lib.mg_tuning_store(C.byref(prob), 1, info.n_pairs, C.byref(t)) == N.MG_OK
+        eng.run(prob)
+        eng.check()
+        out = cube.cpu().numpy().astype(np.float64)
+        shape = (t.kc, t.items_per_sm, t.cost_order)
+        err = np.abs(out - ref).max() / np.abs(ref).max()
+        assert err <= 1e-5, f"shape {shape}: max err / peak {err:.3e}"
+        ferr = abs(flux[0].item() - ref.sum()) / ref.sum()
+        assert ferr <= 1e-6, f"shape {shape}: flux rel err {ferr:.3e}"
+    lib.mg_tuning_reset()
