@@ -691,7 +691,7 @@ int mg_tuning_candidates(int32_t form, mg_tuning* out, int32_t cap) {
   std::vector<mg_tuning> c;
   const bool tc = form == MG_FORM_BF16X3 || form == MG_FORM_F16X3 || form == MG_FORM_BF16X6;
   const int kcs[2] = {0, 32};
-  const int ipss[2] = {ITEMS_PER_SM, ITEMS_PER_SM / 2};
+  const int ipss[3] = {ITEMS_PER_SM, ITEMS_PER_SM / 2, ITEMS_PER_SM / 4};
   for (int kc : kcs) {
     if (kc && !tc) continue;
     for (int ips : ipss)

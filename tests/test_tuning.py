@@ -22,14 +22,14 @@ def _problem(n=1000, nx=64, ny=64, nc=32, form=2, ngal=1):
 def test_candidates_per_form():
     from martini_gb300 import _native as N
     lib = N.load()
-    for form, count, kcs in ((N.MG_FORM_FP32, 4, {0}), (N.MG_FORM_BF16X6, 8, {0, 32}),
-                             (N.MG_FORM_F16X3, 8, {0, 32}), (N.MG_FORM_BF16X3, 8, {0, 32})):
+    for form, count, kcs in ((N.MG_FORM_FP32, 6, {0}), (N.MG_FORM_BF16X6, 12, {0, 32}),
+                             (N.MG_FORM_F16X3, 12, {0, 32}), (N.MG_FORM_BF16X3, 12, {0, 32})):
         out = (N.Tuning * 16)()
         n = lib.mg_tuning_candidates(form, out, 16)
         assert n == count
         shapes = {(t.kc, t.items_per_sm, t.cost_order) for t in out[:n]}
         assert len(shapes) == n and {s[0] for s in shapes} == kcs
-        assert {s[1] for s in shapes} == {24, 12} and {s[2] for s in shapes} == {0, 1}
+        assert {s[1] for s in shapes} == {24, 12, 6} and {s[2] for s in shapes} == {0, 1}
         d = N.Tuning()
         lib.mg_tuning_default(C.byref(d))
         assert (d.kc, d.items_per_sm, d.cost_order) in shapes
