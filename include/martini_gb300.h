@@ -222,7 +222,7 @@ typedef struct mg_tuning {
   int32_t reserved;
 } mg_tuning;
 
-/* The default launch shape: kc 0, 24 items per SM, cost order. */
+/* The default launch shape: kc 0, 6 items per SM, cost order. */
 void mg_tuning_default(mg_tuning* out);
 
 /* Candidate shapes mg_tune times for a form: up to cap into out; returns

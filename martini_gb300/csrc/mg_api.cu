@@ -682,7 +682,9 @@ extern "C" {
 void mg_tuning_default(mg_tuning* out) {
   if (!out) return;
   out->kc = 0;
-  out->items_per_sm = ITEMS_PER_SM;
+  // the autotuner's choice on the single-cube disc workloads; plans keep
+  // ITEMS_PER_SM for their split-K bounds
+  out->items_per_sm = ITEMS_PER_SM / 4;
   out->cost_order = 1;
   out->reserved = 0;
 }

@@ -42,7 +42,7 @@ def test_cache_keys_store_lookup_reset():
     p = _problem()
     got = N.Tuning()
     assert lib.mg_tuning_lookup(p, 1, 200_000, C.byref(got)) == 0
-    assert (got.kc, got.items_per_sm, got.cost_order) == (0, 24, 1)  # the default
+    assert (got.kc, got.items_per_sm, got.cost_order) == (0, 6, 1)  # the default
     t = N.Tuning(32, 12, 0, 0)
     assert lib.mg_tuning_store(p, 1, 200_000, C.byref(t)) == N.MG_OK
     assert lib.mg_tuning_lookup(p, 1, 200_000, C.byref(got)) == 1
